@@ -1,0 +1,361 @@
+"""Benchmark: finite-elasticity assembly throughput (elements/s) on one GB300.
+
+Workload (default): the single-large-mesh configuration — a 32x32x32 box of
+triquadratic Lagrange displacement / trilinear pressure elements (274,625 u
+nodes, 859,812 dofs, 178,723,696 Jacobian nonzeros) with interior nodes
+perturbed by seeded +-0.1h noise, incompressible Mooney-Rivlin c1=2, c2=6.
+One step = one assembly of the mixed-precision Jacobian (FP32 uu block, FP64
+coupling) together with the FP64 residual, at a seeded deformed state (stretch
+1.1, shear 0.05).  All inputs are synthetic; the reference has no dataset for
+this path.
+
+value       elements/s with x resident in device memory (CUDA events around K
+            steps on the launching stream);
+e2e         the same through the C ABI with host (pinned) buffers: the dof
+            vector is copied in and the assembled Jacobian + residual copied
+            out every step;
+roofline    algorithmic bytes of one assembly / its duration, against the
+            measured HBM copy bandwidth;
+cpu_baseline the FP64 CPU oracle (a restatement of the reference's Fortran
+            assembly) on this host's cores, on a bounded sample.
+
+--impl reference runs that CPU restatement alone (all host threads) on the
+same workload and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "assembled elements/s (Jacobian+residual)"
+UNIT = "elements/s"
+
+
+def config_mesh(name):
+    from cm_gb300 import mesh as M
+    if name == "cfg2":
+        m = M.regular_box(32, 32, 32, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0),
+                          perturb=0.1, seed=2)
+        workload = ("32x32x32 triquadratic-u/trilinear-p box, MR c1=2 c2=6, interior nodes +-0.1h, "
+                    "mixed-precision Jacobian + FP64 residual")
+    elif name == "cfg1":
+        m = M.regular_box(4, 4, 4, nxi_u=2, pressure="element", law=M.MR, materials=(2.0, 6.0))
+        workload = "4x4x4 trilinear-u/element-p unit cube, MR c1=2 c2=6, FP64 Jacobian + residual"
+    else:
+        raise SystemExit("unknown config " + name)
+    x = M.deformed_state(m, stretch=1.1, shear=0.05, noise=0.02, pressure=-2.0, seed=4)
+    return m, x, workload
+
+
+def algorithmic_bytes(m, es, mixed):
+    """Bytes one assembly must move: Jacobian values written once (FP32 uu +
+    FP64 coupling for the mixed path, all FP64 otherwise), the residual
+    written once, and the coordinates / dofs / materials read once.  Index
+    arrays are not counted."""
+    rows = es.ndofs
+    if mixed:
+        jac = 4 * es.nnz_uu + 8 * es.nnz_coupling
+    else:
+        jac = 8 * es.nnz
+    inputs = 8 * (3 * m.nu + 3 * m.nu + m.n_pressure) + 8 * m.materials.size
+    return jac + 8 * rows + inputs
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [t.strip() for t in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(m, x, rp1, col1, budget_s=12.0):
+    """The FP64 CPU oracle (restatement of the reference's assembly loop with
+    its bisection CSR add) timed with all host threads on whole assemblies of
+    the same mesh, repeated until about budget_s of CPU work."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    P = oracle.Problem(m)
+    nt = os.cpu_count() or 1
+    import numpy as np
+    vals = np.zeros(int(rp1[-1]) - 1)
+    res = np.zeros(P.ndofs)
+    lib = oracle.lib()
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        rc = lib.or_assemble(P.ref, x.ctypes.data, rp1.ctypes.data, col1.ctypes.data, vals.ctypes.data,
+                             res.ctypes.data, nt)
+        if rc != 0:
+            raise RuntimeError("oracle assembly failed")
+        n += 1
+        if time.perf_counter() - t0 > budget_s or n >= 20:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": n * m.ne / dt, "unit": UNIT, "cores": nt, "kind": "port",
+            "sample": "%d full assemblies (Jacobian+residual, FP64) of the benchmark mesh, %d threads, %.1f s" % (
+                n, nt, dt)}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+    m, x, workload = config_mesh(args.config)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    P = oracle.Problem(m)
+    rp, col = P.pattern()
+    vals = np.zeros(int(rp[-1]) - 1)
+    res = np.zeros(P.ndofs)
+    nt = os.cpu_count() or 1
+    lib = oracle.lib()
+
+    def step():
+        if lib.or_assemble(P.ref, x.ctypes.data, rp.ctypes.data, col.ctypes.data, vals.ctypes.data,
+                           res.ctypes.data, nt) != 0:
+            raise RuntimeError("oracle assembly failed")
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    value = args.steps * m.ne / dt
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload, "elements": m.ne, "dofs": P.ndofs, "nnz": int(rp[-1]) - 1},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port",
+                         "sample": "the full benchmark mesh each step (FP64 restatement of the reference "
+                                   "assembly, element colours split over %d threads)" % nt},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def our_arm(args):
+    import numpy as np
+    import torch
+
+    from cm_gb300 import FiniteElasticityEquationsSet
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    m, x, workload = config_mesh(args.config)
+    mixed = args.config == "cfg2" and not args.fp64
+    es = FiniteElasticityEquationsSet(m)
+    dev = torch.device("cuda", local)
+    xd = torch.from_numpy(x).to(dev)
+    r = torch.empty(es.ndofs, dtype=torch.float64, device=dev)
+    if mixed:
+        vu = torch.empty(es.nnz_uu, dtype=torch.float32, device=dev)
+        vc = torch.empty(es.nnz_coupling, dtype=torch.float64, device=dev)
+        step = lambda: es.jacobian_evaluate_mixed(xd, vu, vc, r)  # noqa: E731
+    else:
+        v = torch.empty(es.nnz, dtype=torch.float64, device=dev)
+        step = lambda: es.jacobian_evaluate(xd, v, r)  # noqa: E731
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        step()
+    es.check_status(xd)
+    torch.cuda.synchronize(dev)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    # device-resident timing
+    l0 = es.launch_count()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for _ in range(args.steps):
+            step()
+        end.record(stream)
+        end.synchronize()
+    launches = es.launch_count() - l0
+    es.check_status(xd)
+    t = start.elapsed_time(end) / 1e3
+    barrier()
+    if dist:
+        tt = torch.tensor([t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    step_s = t / args.steps
+    value = world * m.ne / step_s
+
+    # FP64 path on the same workload (the plain comparator)
+    plain = None
+    if mixed:
+        v64 = torch.empty(es.nnz, dtype=torch.float64, device=dev)
+        es.jacobian_evaluate(xd, v64, r)
+        torch.cuda.synchronize(dev)
+        k64 = max(2, args.steps // 4)
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        for _ in range(k64):
+            es.jacobian_evaluate(xd, v64, r)
+        s1.record(stream)
+        s1.synchronize()
+        t64 = s0.elapsed_time(s1) / 1e3 / k64
+        plain = {"value": m.ne / t64, "unit": UNIT, "ms_per_step": 1e3 * t64, "dtype": "f64",
+                 "roofline_frac_hbm": algorithmic_bytes(m, es, False) / t64 / 1e9 / peaks()["hbm_gbs"]}
+        del v64
+        torch.cuda.empty_cache()
+
+    # end-to-end through the C ABI with pinned host buffers
+    xh = torch.from_numpy(x).pin_memory().numpy()
+    rh = torch.empty(es.ndofs, dtype=torch.float64).pin_memory().numpy()
+    if mixed:
+        vuh = torch.empty(es.nnz_uu, dtype=torch.float32).pin_memory().numpy()
+        vch = torch.empty(es.nnz_coupling, dtype=torch.float64).pin_memory().numpy()
+        e2e_step = lambda: es.jacobian_evaluate_mixed(xh, vuh, vch, rh)  # noqa: E731
+        d2h = 4 * es.nnz_uu + 8 * es.nnz_coupling + 8 * es.ndofs
+    else:
+        vh = torch.empty(es.nnz, dtype=torch.float64).pin_memory().numpy()
+        e2e_step = lambda: es.jacobian_evaluate(xh, vh, rh)  # noqa: E731
+        d2h = 8 * es.nnz + 8 * es.ndofs
+    e2e_step()
+    k_e2e = max(3, min(args.steps, 10))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        e2e_step()
+    te = time.perf_counter() - t0
+    if dist:
+        tt = torch.tensor([te], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        te = float(tt.item())
+    e2e = {"value": world * m.ne * k_e2e / te, "unit": UNIT, "h2d_bytes_per_step": 8 * es.ndofs,
+           "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * te / k_e2e}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    B = algorithmic_bytes(m, es, mixed)
+    pk = peaks()
+    achieved = B / step_s / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get(args.config + ("_mixed" if mixed else "_fp64"))
+        except (ValueError, OSError):
+            traffic = None
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32+fp64" if mixed else "f64", "data": "synthetic",
+        "config": {"workload": workload, "elements": m.ne, "dofs": es.ndofs, "nnz": es.nnz,
+                   "precision": "mixed: FP32 uu tangent, FP64 residual/coupling" if mixed else "FP64",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "working set larger than L2 (Jacobian values %.2f GB)" % (B / 1e9)},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": traffic, "peak_source": pk["source"],
+                     "algorithmic_bytes_per_step": B},
+        "clocks": clk.summary(),
+    }
+    if plain:
+        out["plain_fp64"] = plain
+    if world == 1 and not args.no_cpu:
+        rp1, col1 = es.csr_pattern(base=1)
+        out["cpu_baseline"] = cpu_baseline(m, x, rp1, col1)
+    print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="cfg2", choices=["cfg2", "cfg1"])
+    ap.add_argument("--fp64", action="store_true", help="time the FP64 path instead of the mixed path")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        our_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,61 @@
+// Internal declarations shared by the host set-up (fe_setup.cpp) and the
+// device code / C ABI (fe_kernels.cu) of libcm_fe.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/cm_fe.h"
+
+namespace cmfe {
+
+constexpr int NG = 27;  // 3x3x3 Gauss-Legendre points per element
+
+// Growable-once array without value initialisation (large index arrays are
+// first touched by the threads that fill them).
+template <class T>
+struct RawArray {
+  std::unique_ptr<T[]> p;
+  size_t n = 0;
+  void allocate(size_t count) {
+    p.reset(new T[count]);
+    n = count;
+  }
+  T* data() { return p.get(); }
+  const T* data() const { return p.get(); }
+  size_t size() const { return n; }
+  T& operator[](size_t i) { return p[i]; }
+  const T& operator[](size_t i) const { return p[i]; }
+};
+
+// Everything the device kernels need, built once on the host by fe_create.
+struct HostSetup {
+  int ne = 0, nu = 0, npn = 0;  // elements, u nodes, pressure "row nodes" (p nodes or elements)
+  int n1 = 0, npe = 0, npp = 0; // u nodes per xi, u params per element, p params per element
+  int nr = 0;                   // local row nodes per element: npe + npp
+  int nrow = 0;                 // element dofs: 3*npe + npp
+  int pmode = 0, law = 0, nmat = 0, mat_per_element = 0;
+  bool fibre = false;
+  int64_t ndofs = 0, nnz = 0, nnz_uu = 0, nnz_cp = 0;
+
+  std::vector<int32_t> elem_u, elem_p;   // connectivity (elem_p empty for element-based p)
+  std::vector<double> mat;               // materials
+  std::vector<int32_t> row_ptr;          // 0-based CSR pattern
+  RawArray<int32_t> col;
+  std::vector<int32_t> uu_row_ptr, cp_row_ptr;
+  std::vector<int32_t> wu, wp;           // u-node count of the u-column block of a node's rows
+  int ncolours = 0;
+  std::vector<int32_t> colour_ptr, colour_elems;
+  int ntables = 0;
+  std::vector<uint16_t> tables;          // [ntables][nr][nr]: CSR rank | first-contributor bit 15
+  std::vector<int32_t> elem_table;       // [ne]
+  std::vector<double> geo;               // [ne][NG][10]: dXi/dNu (row-major) and J_x
+  std::vector<double> gbf_u, gbf_p, gw;  // quadrature tables
+};
+
+// Builds the set-up; returns FE_NO_ERROR or a FE_ERR_* code with msg filled.
+int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg);
+
+}  // namespace cmfe

@@ -1,0 +1,1107 @@
+// libcm_fe: GB300 (sm_103a) finite-elasticity element assembly and the C ABI
+// declared in include/cm_fe.h.
+//
+// One CTA assembles one element at a time (persistent over the elements of
+// one colour).  Per element:
+//   P0  gather the deformed coordinates z and pressures of the element;
+//   P1  interpolate dz/dxi at the 27 Gauss points (243 independent sums);
+//   P2  per Gauss point: metrics, F, Cauchy stress and spatial tangent
+//       (FINITE_ELASTICITY_GAUSS_STRESS_TENSOR / _ELASTICITY_TENSOR);
+//   P3  dN/dz at every Gauss point (DPHIDZ);
+//   P4  residual rows, accumulated over Gauss points in the reference order;
+//   P5  lower-triangle Jacobian entries held in registers, accumulated over
+//       Gauss points in the reference order (per Gauss point the 3-vectors
+//       JGW*(c + sigma)*dN/dz of every column are formed once in shared
+//       memory, then each entry adds one 3-term dot product);
+//   P6  scatter into the CSR values and the residual (each entry and its
+//       mirror; first contributor in colour order stores, later ones add).
+// Elements of one colour share no node, so P6 needs no atomics and the
+// result does not depend on scheduling.
+//
+// The mixed-precision variant keeps P1-P4 and the pressure coupling in FP64
+// and runs the tangent (elasticity tensor, uu block) in FP32.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <type_traits>
+
+#include "fe_internal.h"
+
+using cmfe::HostSetup;
+using cmfe::NG;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                           \
+  do {                                                                                           \
+    cudaError_t err__ = (expr);                                                                  \
+    if (err__ != cudaSuccess)                                                                    \
+      return set_error(FE_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(err__));      \
+  } while (0)
+
+// ------------------------------------------------------------ constants ----
+__constant__ int c_T2V[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};   // TENSOR_TO_VOIGT3
+__constant__ int c_V2T[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};  // VOIGT_TO_TENSOR3
+
+constexpr double ZERO_TOL = 5.0 * 2.220446049250313e-16;  // ZERO_TOLERANCE (constants.f90:68)
+
+enum Mode { M_RES = 0, M_JAC = 1, M_MIX = 2, M_ERES = 3, M_EJAC = 4 };
+
+struct KParams {
+  int nu, law, nmat, matpe;
+  const int32_t* elem_u;
+  const int32_t* elem_p;
+  const double* geo;
+  const double* mat;
+  const double* gbf_u;
+  const double* gbf_p;
+  const double* gw;
+  const int32_t* row_ptr;
+  const int32_t* uu_row_ptr;
+  const int32_t* cp_row_ptr;
+  const int32_t* wu;
+  const int32_t* wp;
+  const uint16_t* tables;
+  const int32_t* elem_table;
+  const int32_t* elems;  // element list of this launch (NULL: first_elem + i)
+  int count;
+  int first_elem;
+  const double* x;
+  double* r;
+  double* vals;      // FP64 CSR values, or FP64 coupling values (mixed)
+  float* vals_uu;    // FP32 uu values (mixed)
+  double* elem_out;  // element-level output
+  unsigned* status;
+};
+
+template <int N1, int PM>
+struct Cfg {
+  static constexpr int NPE = N1 * N1 * N1;
+  static constexpr int NPP = PM ? 8 : 1;
+  static constexpr int NR = NPE + NPP;
+  static constexpr int NU3 = 3 * NPE;
+  static constexpr int NROW = NU3 + NPP;
+  static constexpr int NUU = NU3 * (NU3 + 1) / 2;
+  static constexpr int NPU = NPP * NU3;
+  static constexpr int THREADS = 128;
+  static constexpr int EUU = (NUU + THREADS - 1) / THREADS;
+  static constexpr int EPU = (NPU + THREADS - 1) / THREADS;
+  static constexpr int GPS = 60;  // per-Gauss-point record, doubles
+  // shared-memory layout (doubles)
+  static constexpr int O_GBF = 0;
+  static constexpr int O_GBFP = O_GBF + NG * 4 * NPE;
+  static constexpr int O_W = O_GBFP + NG * 8;
+  static constexpr int O_Z = O_W + NG;
+  static constexpr int O_P = O_Z + 3 * NPE;
+  static constexpr int O_DZ = O_P + 8;
+  static constexpr int O_PG = O_DZ + NG * 9;
+  static constexpr int O_GP = O_PG + NG;
+  static constexpr int O_DPHI = O_GP + NG * GPS;
+  static constexpr int O_T = O_DPHI + NG * NPE * 3;
+  static constexpr int O_END = O_T + 6 * NPE * 3;
+  static constexpr size_t SMEM = O_END * sizeof(double) + (NR + 4) * sizeof(int);
+};
+
+// ------------------------------------------------------- device maths ----
+__device__ __forceinline__ void d_inv3(const double a[3][3], double b[3][3], double& det) {
+  det = a[0][0] * a[1][1] * a[2][2] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
+        a[0][0] * a[2][1] * a[1][2] - a[1][0] * a[0][1] * a[2][2] - a[2][0] * a[1][1] * a[0][2];
+  if (fabs(det) > ZERO_TOL) {
+    b[0][0] = (a[1][1] * a[2][2] - a[2][1] * a[1][2]) / det;
+    b[1][0] = (a[1][2] * a[2][0] - a[2][2] * a[1][0]) / det;
+    b[2][0] = (a[1][0] * a[2][1] - a[2][0] * a[1][1]) / det;
+    b[0][1] = (a[2][1] * a[0][2] - a[0][1] * a[2][2]) / det;
+    b[1][1] = (a[2][2] * a[0][0] - a[0][2] * a[2][0]) / det;
+    b[2][1] = (a[2][0] * a[0][1] - a[0][0] * a[2][1]) / det;
+    b[0][2] = (a[0][1] * a[1][2] - a[1][1] * a[0][2]) / det;
+    b[1][2] = (a[0][2] * a[1][0] - a[1][2] * a[0][0]) / det;
+    b[2][2] = (a[0][0] * a[1][1] - a[1][0] * a[0][1]) / det;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) b[i][j] = 0.0;
+  }
+}
+
+template <class T>
+__device__ __forceinline__ T d_pow_m13(T j);
+template <>
+__device__ __forceinline__ double d_pow_m13<double>(double j) { return pow(j, -1.0 / 3.0); }
+template <>
+__device__ __forceinline__ float d_pow_m13<float>(float j) { return powf(j, -1.0f / 3.0f); }
+template <class T>
+__device__ __forceinline__ T d_exp(T v);
+template <>
+__device__ __forceinline__ double d_exp<double>(double v) { return exp(v); }
+template <>
+__device__ __forceinline__ float d_exp<float>(float v) { return expf(v); }
+
+// Push-forward matrix t(F) of FINITE_ELASTICITY_PUSH_*_TENSOR (:1182-1253).
+template <class T>
+__device__ __forceinline__ void d_push_t(const T F[3][3], T t[6][6]) {
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 6; ++i) t[i][j] = F[c_V2T[i][0]][c_V2T[j][0]] * F[c_V2T[i][1]][c_V2T[j][1]];
+#pragma unroll
+  for (int j = 3; j < 6; ++j)
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+      t[i][j] = F[c_V2T[i][0]][c_V2T[j][0]] * F[c_V2T[i][1]][c_V2T[j][1]] +
+                F[c_V2T[i][0]][c_V2T[j][1]] * F[c_V2T[i][1]][c_V2T[j][0]];
+}
+
+// F_bar = F J^(-1/3), AZL = F_bar^T F_bar, and the fictitious 2nd Piola
+// stress (and material tangent when C != nullptr) of MR (:4386-4394,
+// :684-699) or Guccione (:4419-4424, :758-781).
+template <class T>
+__device__ void d_fictitious(int law, const T* c, const T F[3][3], T J, T mod[3][3], T S[6], T (*C)[6]) {
+  const T s = d_pow_m13<T>(J);
+  T azl[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) mod[i][j] = F[i][j] * s;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) azl[i][j] = mod[0][i] * mod[0][j] + mod[1][i] * mod[1][j] + mod[2][i] * mod[2][j];
+  if (law == FE_LAW_MOONEY_RIVLIN) {
+    const T I1 = azl[0][0] + azl[1][1] + azl[2][2];
+    const T t1 = T(-2.0) * c[1];
+    const T t2 = T(2.0) * (c[0] + I1 * c[1]);
+    S[0] = t1 * azl[0][0] + t2;
+    S[1] = t1 * azl[1][1] + t2;
+    S[2] = t1 * azl[2][2] + t2;
+    S[3] = t1 * azl[1][0];
+    S[4] = t1 * azl[2][0];
+    S[5] = t1 * azl[2][1];
+    if (C) {
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 6; ++j) C[i][j] = T(0);
+      const T a = T(4.0) * c[1], b = T(-2.0) * c[1];
+      C[1][0] = a; C[2][0] = a; C[0][1] = a; C[2][1] = a; C[0][2] = a; C[1][2] = a;
+      C[3][3] = b; C[4][4] = b; C[5][5] = b;
+    }
+  } else {
+    const T B[6] = {T(2.0) * c[1], T(2.0) * c[2], T(2.0) * c[2], c[3], c[3], c[2]};
+    const T E[6] = {T(0.5) * (azl[0][0] - T(1.0)), T(0.5) * (azl[1][1] - T(1.0)), T(0.5) * (azl[2][2] - T(1.0)),
+                    azl[1][0], azl[2][0], azl[2][1]};
+    T DQ[6];
+    T dot = T(0);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) DQ[i] = B[i] * E[i];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) dot = dot + E[i] * DQ[i];
+    const T t1 = T(0.5) * c[0] * d_exp<T>(T(0.5) * dot);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) S[i] = t1 * DQ[i];
+    if (C) {
+#pragma unroll
+      for (int j = 0; j < 6; ++j)
+#pragma unroll
+        for (int i = j; i < 6; ++i) C[i][j] = t1 * DQ[i] * DQ[j];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) C[i][i] = C[i][i] + t1 * B[i];
+#pragma unroll
+      for (int j = 1; j < 6; ++j)
+#pragma unroll
+        for (int i = 0; i < j; ++i) C[i][j] = C[j][i];
+    }
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void d_push_stress(T S[6], const T t[6][6], T J) {
+  T r[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    T s = T(0);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) s = s + t[i][j] * S[j];
+    r[i] = s;
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) S[i] = r[i] / J;
+}
+
+// FINITE_ELASTICITY_GAUSS_STRESS_TENSOR (:4342-4454): Cauchy stress (Voigt).
+__device__ void d_gauss_stress(int law, const double* c, const double F[3][3], double J, double p, double S[6]) {
+  double mod[3][3], t[6][6];
+  d_fictitious<double>(law, c, F, J, mod, S, nullptr);
+  d_push_t<double>(mod, t);
+  d_push_stress<double>(S, t, J);
+  const double ot = (S[0] + S[1] + S[2]) / 3.0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) S[i] = S[i] - ot + p;
+}
+
+// FINITE_ELASTICITY_GAUSS_ELASTICITY_TENSOR (:609-835): spatial tangent and
+// Cauchy stress (Voigt), in precision T.
+template <class T>
+__device__ void d_gauss_elasticity(int law, const T* c, const T F[3][3], T J, T p, T C[6][6], T S[6]) {
+  const T ONETHIRD = T(1.0) / T(3.0), TWOTHIRDS = T(2.0) / T(3.0);
+  const T DP[3][3] = {{TWOTHIRDS, -ONETHIRD, -ONETHIRD}, {-ONETHIRD, TWOTHIRDS, -ONETHIRD},
+                      {-ONETHIRD, -ONETHIRD, TWOTHIRDS}};
+  T mod[3][3], t[6][6];
+  d_fictitious<T>(law, c, F, J, mod, S, C);
+  d_push_t<T>(mod, t);
+  d_push_stress<T>(S, t, J);
+  {  // C <- t C t^T / J
+    T A[6][6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        T s = T(0);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s = s + t[i][k] * C[k][j];
+        A[i][j] = s;
+      }
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        T s = T(0);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s = s + A[i][k] * t[j][k];
+        C[i][j] = s / J;
+      }
+  }
+  const T trace = S[0] + S[1] + S[2];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) S[i] = S[i] - ONETHIRD * trace;
+  const T tt = TWOTHIRDS * trace;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) C[i][i] = C[i][i] + tt * (i < 3 ? T(1.0) : T(0.5));
+  T M[3][3], N[3][3], Q[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) s = s + C[i][k] * DP[k][j];
+      M[i][j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) s = s + DP[i][k] * M[k][j];
+      N[i][j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) s = s + DP[i][k] * C[k][3 + j];
+      Q[i][j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      C[i][j] = N[i][j];
+      C[i][3 + j] = Q[i][j];
+      C[3 + j][i] = Q[i][j];
+    }
+#pragma unroll
+  for (int j = 0; j < 6; ++j)
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const T ui = i < 3 ? TWOTHIRDS : T(0), uj = j < 3 ? TWOTHIRDS : T(0);
+      C[i][j] = C[i][j] - (ui * S[j] + uj * S[i]);
+    }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) S[i] = S[i] + p;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) C[i][i] = C[i][i] - p;
+  C[1][0] = C[1][0] + p; C[2][0] = C[2][0] + p; C[0][1] = C[0][1] + p;
+  C[2][1] = C[2][1] + p; C[0][2] = C[0][2] + p; C[1][2] = C[1][2] + p;
+}
+
+// Block index of the (row comp m, col comp n) tempvec block: 0..2 diagonal,
+// 3,4,5 for (n,m) = (0,1), (0,2), (1,2).
+__device__ __forceinline__ int blk_of(int m, int n) { return m == n ? n : (n == 0 ? (m == 1 ? 3 : 4) : 5); }
+
+// ---------------------------------------------------------- the kernel ----
+template <int N1, int PM, int MODE>
+__global__ void __launch_bounds__(128) fe_element_kernel(KParams P) {
+  using C = Cfg<N1, PM>;
+  constexpr int NPE = C::NPE, NPP = C::NPP, NR = C::NR, NU3 = C::NU3, NROW = C::NROW;
+  constexpr bool JAC = (MODE == M_JAC || MODE == M_MIX || MODE == M_EJAC);
+  constexpr bool MIX = (MODE == M_MIX);
+  using TT = typename std::conditional<MIX, float, double>::type;  // tangent precision
+  extern __shared__ __align__(16) double smem[];
+  double* s_gbf = smem + C::O_GBF;
+  double* s_gbfp = smem + C::O_GBFP;
+  double* s_w = smem + C::O_W;
+  double* s_z = smem + C::O_Z;
+  double* s_p = smem + C::O_P;
+  double* s_dz = smem + C::O_DZ;
+  double* s_pg = smem + C::O_PG;
+  double* s_gp = smem + C::O_GP;
+  double* s_dphi = smem + C::O_DPHI;
+  TT* s_T = reinterpret_cast<TT*>(smem + C::O_T);
+  int* s_node = reinterpret_cast<int*>(smem + C::O_END);  // [NR] row nodes, then table id
+  const int tid = threadIdx.x;
+  const bool want_res = (MODE == M_RES || MODE == M_ERES || P.r != nullptr) && MODE != M_EJAC;
+
+  for (int i = tid; i < NG * 4 * NPE; i += C::THREADS) s_gbf[i] = P.gbf_u[i];
+  for (int i = tid; i < NG * 8; i += C::THREADS) s_gbfp[i] = P.gbf_p[i];
+  for (int i = tid; i < NG; i += C::THREADS) s_w[i] = P.gw[i];
+
+  // Per-thread Jacobian entry descriptors: uu lower triangle in row-major
+  // order (row R, col Cc <= R over the 3*NPE displacement dofs), then the
+  // pressure-row x displacement-column block.
+  int e_uu[C::EUU];
+  int e_pu[C::EPU];
+  if (JAC) {
+#pragma unroll
+    for (int j = 0; j < C::EUU; ++j) {
+      const int k = tid + j * C::THREADS;
+      if (k < C::NUU) {
+        int R = (int)((sqrtf(8.0f * (float)k + 1.0f) - 1.0f) * 0.5f);
+        while (R * (R + 1) / 2 > k) --R;
+        while ((R + 1) * (R + 2) / 2 <= k) ++R;
+        const int Cc = k - R * (R + 1) / 2;
+        e_uu[j] = (R << 8) | Cc;
+      } else {
+        e_uu[j] = -1;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < C::EPU; ++j) {
+      const int k = tid + j * C::THREADS;
+      e_pu[j] = (k < C::NPU) ? (((k / NU3) << 8) | (k % NU3)) : -1;
+    }
+  }
+
+  for (int it = blockIdx.x; it < P.count; it += gridDim.x) {
+    const int e = P.elems ? P.elems[it] : P.first_elem + it;
+    __syncthreads();  // previous element done with shared memory
+    // P0: gather
+    if (tid < NPE) s_node[tid] = P.elem_u[(size_t)e * NPE + tid];
+    if (tid >= NPE && tid < NR) s_node[tid] = PM ? P.elem_p[(size_t)e * 8 + (tid - NPE)] : e;
+    if (tid == NR) s_node[NR] = P.elem_table[e];
+    __syncthreads();
+    for (int i = tid; i < 3 * NPE; i += C::THREADS) {
+      const int c = i / NPE, a = i % NPE;
+      s_z[c * NPE + a] = P.x[(size_t)c * P.nu + s_node[a]];
+    }
+    if (tid < NPP) s_p[tid] = P.x[(size_t)3 * P.nu + s_node[NPE + tid]];
+    __syncthreads();
+    // P1: dz/dxi at every Gauss point; pressure at every Gauss point
+    for (int i = tid; i < NG * 9; i += C::THREADS) {
+      const int g = i / 9, c = (i / 3) % 3, k = i % 3;
+      const double* gb = &s_gbf[(g * 4 + k + 1) * NPE];
+      const double* zc = &s_z[c * NPE];
+      double acc = 0.0;
+#pragma unroll 9
+      for (int a = 0; a < NPE; ++a) acc = acc + gb[a] * zc[a];
+      s_dz[i] = acc;
+    }
+    if (tid < NG) {
+      double pg;
+      if (PM) {
+        pg = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) pg = pg + s_gbfp[tid * 8 + q] * s_p[q];
+      } else {
+        pg = s_p[0];
+      }
+      s_pg[tid] = pg;
+    }
+    __syncthreads();
+    // P2: per Gauss point kinematics and constitutive law
+    if (tid < NG) {
+      const int g = tid;
+      double dz[3][3], dxi[3][3], det_dz, gl[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dz[c][k] = s_dz[g * 9 + c * 3 + k];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) gl[i][j] = dz[0][i] * dz[0][j] + dz[1][i] * dz[1][j] + dz[2][i] * dz[2][j];
+      const double det_gl = gl[0][0] * gl[1][1] * gl[2][2] + gl[0][1] * gl[1][2] * gl[2][0] +
+                            gl[0][2] * gl[1][0] * gl[2][1] - gl[0][0] * gl[2][1] * gl[1][2] -
+                            gl[1][0] * gl[0][1] * gl[2][2] - gl[2][0] * gl[1][1] * gl[0][2];
+      const double jz = sqrt(fabs(det_gl));
+      d_inv3(dz, dxi, det_dz);
+      const double* geo = &P.geo[((size_t)e * NG + g) * 10];
+      double dn[3][3], F[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) dn[i][j] = geo[i * 3 + j];
+      const double jx = geo[9];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) F[i][j] = dz[i][0] * dn[0][j] + dz[i][1] * dn[1][j] + dz[i][2] * dn[2][j];
+      const double jznu = jz / jx;
+      double* rec = &s_gp[g * C::GPS];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) rec[i * 3 + j] = dxi[i][j];
+      rec[9] = jz * s_w[g];
+      rec[10] = jx * s_w[g];
+      rec[11] = jznu;
+      const double* cm = P.mat + (P.matpe ? (size_t)e * P.nmat : 0);
+      double cc[4] = {cm[0], cm[1], P.nmat > 2 ? cm[2] : 0.0, P.nmat > 3 ? cm[3] : 0.0};
+      const double pg = s_pg[g];
+      bool ok = (det_dz > 0.0) && (jznu > 0.0);
+      if (want_res) {
+        double S[6];
+        d_gauss_stress(P.law, cc, F, jznu, pg, S);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+          rec[12 + i] = S[i];
+          ok = ok && isfinite(S[i]);
+        }
+      }
+      if (JAC) {
+        TT Ct[6][6], St[6], Ft[3][3], ct[4];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) Ft[i][j] = (TT)F[i][j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) ct[i] = (TT)cc[i];
+        d_gauss_elasticity<TT>(P.law, ct, Ft, (TT)jznu, (TT)pg, Ct, St);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+          rec[18 + i] = (double)St[i];
+          ok = ok && isfinite((double)St[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+          for (int j = 0; j < 6; ++j) rec[24 + i * 6 + j] = (double)Ct[i][j];
+      }
+      if (!ok) atomicOr(P.status, 1u);
+    }
+    __syncthreads();
+    // P3: DPHIDZ[g][a][mh] = sum_ni dN_a/dxi_ni * dxi_ni/dz_mh
+    for (int i = tid; i < NG * NPE * 3; i += C::THREADS) {
+      const int g = i / (NPE * 3), a = (i / 3) % NPE, mh = i % 3;
+      const double* rec = &s_gp[g * C::GPS];
+      double s = 0.0;
+#pragma unroll
+      for (int ni = 0; ni < 3; ++ni) s = s + s_gbf[(g * 4 + ni + 1) * NPE + a] * rec[ni * 3 + mh];
+      s_dphi[i] = s;
+    }
+    __syncthreads();
+    const uint16_t* tab = P.tables + (size_t)s_node[NR] * NR * NR;
+    // P4: residual
+    if (want_res && tid < NROW) {
+      double acc = 0.0;
+      if (tid < NU3) {
+        const int m = tid / NPE, a = tid % NPE;
+        for (int g = 0; g < NG; ++g) {
+          const double* rec = &s_gp[g * C::GPS];
+          const double* dp = &s_dphi[(g * NPE + a) * 3];
+          const double jgw = rec[9];
+          const double d = dp[0] * (jgw * rec[12 + c_T2V[0][m]]) + dp[1] * (jgw * rec[12 + c_T2V[1][m]]) +
+                           dp[2] * (jgw * rec[12 + c_T2V[2][m]]);
+          acc = acc + d;
+        }
+      } else {
+        const int q = tid - NU3;
+        for (int g = 0; g < NG; ++g) {
+          const double* rec = &s_gp[g * C::GPS];
+          const double t1 = rec[10] * (rec[11] - 1.0);
+          acc = PM ? acc + t1 * s_gbfp[g * 8 + q] : acc + t1;
+        }
+      }
+      if (MODE == M_ERES) {
+        P.elem_out[(size_t)(it)*NROW + tid] = acc;
+      } else {
+        const int ln = tid < NU3 ? tid % NPE : NPE + (tid - NU3);
+        const size_t R = tid < NU3 ? (size_t)(tid / NPE) * P.nu + s_node[ln] : (size_t)3 * P.nu + s_node[ln];
+        const bool first = tab[ln * NR + ln] & 0x8000;
+        P.r[R] = first ? acc : P.r[R] + acc;
+      }
+    }
+    if (!JAC) continue;
+    // P5: Jacobian entries
+    TT acc_uu[C::EUU];
+    double acc_pu[C::EPU];
+#pragma unroll
+    for (int j = 0; j < C::EUU; ++j) acc_uu[j] = TT(0);
+#pragma unroll
+    for (int j = 0; j < C::EPU; ++j) acc_pu[j] = 0.0;
+    for (int g = 0; g < NG; ++g) {
+      const double* rec = &s_gp[g * C::GPS];
+      const double* dpg = &s_dphi[g * NPE * 3];
+      // a) tempvecs TEMPVEC = JGW_SUB_MAT * DPHIDZ(:,ns,nh) for the six blocks
+      for (int i = tid; i < 6 * NPE; i += C::THREADS) {
+        const int blk = i / NPE, b = i % NPE;
+        const int nh = blk < 3 ? blk : (blk == 5 ? 1 : 0);
+        const int mh = blk < 3 ? blk : (blk == 3 ? 1 : 2);
+        const TT jgw = (TT)rec[9];
+        TT sub[3][3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const TT cv = (TT)rec[24 + c_T2V[r][mh] * 6 + c_T2V[c][nh]];
+            sub[r][c] = blk < 3 ? jgw * (cv + (TT)rec[18 + c_T2V[r][c]]) : jgw * cv;
+          }
+        const TT d0 = (TT)dpg[b * 3 + 0], d1 = (TT)dpg[b * 3 + 1], d2 = (TT)dpg[b * 3 + 2];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) s_T[i * 3 + r] = sub[r][0] * d0 + sub[r][1] * d1 + sub[r][2] * d2;
+      }
+      __syncthreads();
+      // b) K(row, col) += DOT_PRODUCT(DPHIDZ(:,ms,mh), TEMPVEC)
+#pragma unroll
+      for (int j = 0; j < C::EUU; ++j) {
+        const int d = e_uu[j];
+        if (d >= 0) {
+          const int R = d >> 8, Cc = d & 0xff;
+          const int m = R / NPE, a = R % NPE, n = Cc / NPE, b = Cc % NPE;
+          const TT* tv = &s_T[(blk_of(m, n) * NPE + b) * 3];
+          const TT d0 = (TT)dpg[a * 3 + 0], d1 = (TT)dpg[a * 3 + 1], d2 = (TT)dpg[a * 3 + 2];
+          acc_uu[j] = acc_uu[j] + (d0 * tv[0] + d1 * tv[1] + d2 * tv[2]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < C::EPU; ++j) {
+        const int d = e_pu[j];
+        if (d >= 0) {
+          const int q = d >> 8, Cc = d & 0xff;
+          const int n = Cc / NPE, b = Cc % NPE;
+          const double jd = rec[9] * dpg[b * 3 + n];
+          acc_pu[j] = PM ? acc_pu[j] + jd * s_gbfp[g * 8 + q] : acc_pu[j] + jd;
+        }
+      }
+      __syncthreads();
+    }
+    // P6: scatter the entries and their mirrors
+    if (MODE == M_EJAC) {
+      double* out = P.elem_out + (size_t)it * NROW * NROW;
+#pragma unroll
+      for (int j = 0; j < C::EUU; ++j) {
+        const int d = e_uu[j];
+        if (d >= 0) {
+          const int R = d >> 8, Cc = d & 0xff;
+          out[(size_t)Cc * NROW + R] = (double)acc_uu[j];
+          out[(size_t)R * NROW + Cc] = (double)acc_uu[j];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < C::EPU; ++j) {
+        const int d = e_pu[j];
+        if (d >= 0) {
+          const int R = NU3 + (d >> 8), Cc = d & 0xff;
+          out[(size_t)Cc * NROW + R] = acc_pu[j];
+          out[(size_t)R * NROW + Cc] = acc_pu[j];
+        }
+      }
+      for (int i = tid; i < NPP * NPP; i += C::THREADS) out[(size_t)(NU3 + i / NPP) * NROW + NU3 + i % NPP] = 0.0;
+      continue;
+    }
+    const int nu = P.nu;
+#pragma unroll
+    for (int j = 0; j < C::EUU; ++j) {
+      const int d = e_uu[j];
+      if (d >= 0) {
+        const int R = d >> 8, Cc = d & 0xff;
+        const int m = R / NPE, a = R % NPE, n = Cc / NPE, b = Cc % NPE;
+        const int na = s_node[a], nb = s_node[b];
+        const uint16_t tab_ab = tab[a * NR + b], tab_ba = tab[b * NR + a];
+        const TT v = acc_uu[j];
+        if (MIX) {
+          const size_t p1 = (size_t)P.uu_row_ptr[(size_t)m * nu + na] + (size_t)n * P.wu[na] + (tab_ab & 0x7fff);
+          P.vals_uu[p1] = (tab_ab & 0x8000) ? (float)v : P.vals_uu[p1] + (float)v;
+          if (R != Cc) {
+            const size_t p2 = (size_t)P.uu_row_ptr[(size_t)n * nu + nb] + (size_t)m * P.wu[nb] + (tab_ba & 0x7fff);
+            P.vals_uu[p2] = (tab_ba & 0x8000) ? (float)v : P.vals_uu[p2] + (float)v;
+          }
+        } else {
+          const size_t p1 = (size_t)P.row_ptr[(size_t)m * nu + na] + (size_t)n * P.wu[na] + (tab_ab & 0x7fff);
+          P.vals[p1] = (tab_ab & 0x8000) ? (double)v : P.vals[p1] + (double)v;
+          if (R != Cc) {
+            const size_t p2 = (size_t)P.row_ptr[(size_t)n * nu + nb] + (size_t)m * P.wu[nb] + (tab_ba & 0x7fff);
+            P.vals[p2] = (tab_ba & 0x8000) ? (double)v : P.vals[p2] + (double)v;
+          }
+        }
+      }
+    }
+    const int32_t* rp = MIX ? P.cp_row_ptr : P.row_ptr;
+#pragma unroll
+    for (int j = 0; j < C::EPU; ++j) {
+      const int d = e_pu[j];
+      if (d >= 0) {
+        const int q = d >> 8, Cc = d & 0xff;
+        const int n = Cc / NPE, b = Cc % NPE;
+        const int lq = NPE + q;
+        const int pq = s_node[lq], nb = s_node[b];
+        const uint16_t t_qb = tab[lq * NR + b], t_bq = tab[b * NR + lq];
+        const double v = acc_pu[j];
+        const size_t p1 = (size_t)rp[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (t_qb & 0x7fff);
+        P.vals[p1] = (t_qb & 0x8000) ? v : P.vals[p1] + v;
+        // mirror: displacement row (n, b), pressure column q
+        const size_t p2 = MIX ? (size_t)rp[(size_t)n * nu + nb] + (t_bq & 0x7fff)
+                              : (size_t)rp[(size_t)n * nu + nb] + 3 * (size_t)P.wu[nb] + (t_bq & 0x7fff);
+        P.vals[p2] = (t_bq & 0x8000) ? v : P.vals[p2] + v;
+      }
+    }
+    // structurally zero pressure-pressure entries: stored by their first contributor
+    for (int i = tid; i < NPP * NPP; i += C::THREADS) {
+      const int lq = NPE + i / NPP, lq2 = NPE + i % NPP;
+      const uint16_t t = tab[lq * NR + lq2];
+      if (t & 0x8000) {
+        const int pq = s_node[lq];
+        const size_t pos = MIX ? (size_t)rp[(size_t)3 * nu + pq] + 3 * (size_t)P.wp[pq] + (t & 0x7fff)
+                               : (size_t)rp[(size_t)3 * nu + pq] + 3 * (size_t)P.wp[pq] + (t & 0x7fff);
+        P.vals[pos] = 0.0;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------ handle ----
+template <class T>
+int dev_upload(T** dst, const std::vector<T>& src) {
+  *dst = nullptr;
+  if (src.empty()) return FE_NO_ERROR;
+  CUDA_TRY(cudaMalloc(dst, src.size() * sizeof(T)));
+  CUDA_TRY(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return FE_NO_ERROR;
+}
+
+}  // namespace
+
+struct fe_equations_set {
+  HostSetup hs;
+  int device = 0;
+  int num_sms = 0;
+  int32_t *d_elem_u = nullptr, *d_elem_p = nullptr, *d_row_ptr = nullptr, *d_uu_row_ptr = nullptr,
+          *d_cp_row_ptr = nullptr, *d_wu = nullptr, *d_wp = nullptr, *d_elem_table = nullptr,
+          *d_colour_elems = nullptr;
+  uint16_t* d_tables = nullptr;
+  double *d_geo = nullptr, *d_mat = nullptr, *d_gbf_u = nullptr, *d_gbf_p = nullptr, *d_gw = nullptr;
+  unsigned* d_status = nullptr;
+  // staging for calls given host memory
+  double *s_x = nullptr, *s_r = nullptr, *s_vals = nullptr, *s_cp = nullptr, *s_elem = nullptr;
+  float* s_uu = nullptr;
+  size_t s_elem_bytes = 0;
+  int64_t launches = 0;
+  std::mutex mu;
+};
+
+namespace {
+
+template <int N1, int PM, int MODE>
+int launch_t(fe_handle h, KParams& kp, cudaStream_t st) {
+  using C = Cfg<N1, PM>;
+  static bool attr_done[64] = {false};
+  auto kern = fe_element_kernel<N1, PM, MODE>;
+  const int dev = h->device;
+  if (!attr_done[dev & 63]) {
+    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+    attr_done[dev & 63] = true;
+  }
+  int per_sm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::THREADS, C::SMEM));
+  if (per_sm < 1) per_sm = 1;
+  const int grid = std::max(1, std::min(kp.count, per_sm * h->num_sms));
+  kern<<<grid, C::THREADS, C::SMEM, st>>>(kp);
+  CUDA_TRY(cudaGetLastError());
+  h->launches++;
+  return FE_NO_ERROR;
+}
+
+template <int MODE>
+int launch(fe_handle h, KParams& kp, cudaStream_t st) {
+  const auto& s = h->hs;
+  if (kp.count <= 0) return FE_NO_ERROR;
+  if (s.n1 == 2 && s.pmode == 0) return launch_t<2, 0, MODE>(h, kp, st);
+  if (s.n1 == 2 && s.pmode == 1) return launch_t<2, 1, MODE>(h, kp, st);
+  if (s.n1 == 3 && s.pmode == 0) return launch_t<3, 0, MODE>(h, kp, st);
+  return launch_t<3, 1, MODE>(h, kp, st);
+}
+
+KParams base_params(fe_handle h) {
+  KParams k;
+  std::memset(&k, 0, sizeof(k));
+  const auto& s = h->hs;
+  k.nu = s.nu;
+  k.law = s.law;
+  k.nmat = s.nmat;
+  k.matpe = s.mat_per_element;
+  k.elem_u = h->d_elem_u;
+  k.elem_p = h->d_elem_p;
+  k.geo = h->d_geo;
+  k.mat = h->d_mat;
+  k.gbf_u = h->d_gbf_u;
+  k.gbf_p = h->d_gbf_p;
+  k.gw = h->d_gw;
+  k.row_ptr = h->d_row_ptr;
+  k.uu_row_ptr = h->d_uu_row_ptr;
+  k.cp_row_ptr = h->d_cp_row_ptr;
+  k.wu = h->d_wu;
+  k.wp = h->d_wp;
+  k.tables = h->d_tables;
+  k.elem_table = h->d_elem_table;
+  k.status = h->d_status;
+  return k;
+}
+
+// Colour-by-colour launches over all elements.
+template <int MODE>
+int run_colours(fe_handle h, KParams kp, cudaStream_t st) {
+  const auto& s = h->hs;
+  for (int c = 0; c < s.ncolours; ++c) {
+    kp.elems = h->d_colour_elems + s.colour_ptr[c];
+    kp.count = s.colour_ptr[c + 1] - s.colour_ptr[c];
+    int rc = launch<MODE>(h, kp, st);
+    if (rc) return rc;
+  }
+  return FE_NO_ERROR;
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int ensure(void** buf, size_t bytes) {
+  if (*buf) return FE_NO_ERROR;
+  cudaError_t e = cudaMalloc(buf, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *buf = nullptr;
+    return set_error(FE_ERR_OUT_OF_MEMORY, std::string("device staging allocation failed: ") + cudaGetErrorString(e));
+  }
+  return FE_NO_ERROR;
+}
+
+int check_handle(fe_handle h) {
+  if (!h) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL handle");
+  int cur = 0;
+  CUDA_TRY(cudaGetDevice(&cur));
+  if (cur != h->device) return set_error(FE_ERR_INVALID_ARGUMENT, "handle belongs to another CUDA device");
+  return FE_NO_ERROR;
+}
+
+// Stages x to the device if it is host memory.
+int stage_in(fe_handle h, const double* x, const double** dx, cudaStream_t st, bool* host) {
+  *host = !is_device_ptr(x);
+  if (!*host) {
+    *dx = x;
+    return FE_NO_ERROR;
+  }
+  int rc = ensure((void**)&h->s_x, sizeof(double) * h->hs.ndofs);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(h->s_x, x, sizeof(double) * h->hs.ndofs, cudaMemcpyHostToDevice, st));
+  *dx = h->s_x;
+  return FE_NO_ERROR;
+}
+
+int finish_status(fe_handle h, cudaStream_t st) {
+  unsigned v = 0;
+  CUDA_TRY(cudaMemcpyAsync(&v, h->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemsetAsync(h->d_status, 0, sizeof(unsigned), st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (v) return set_error(FE_ERR_NUMERICAL, "a Gauss point had det F <= 0 or a non-finite stress");
+  return FE_NO_ERROR;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fe_last_error(char* buf, int32_t size) {
+  if (!buf || size <= 0) return FE_ERR_INVALID_ARGUMENT;
+  std::snprintf(buf, (size_t)size, "%s", g_last_error.c_str());
+  return FE_NO_ERROR;
+}
+
+int fe_create(const fe_mesh_desc* desc, fe_handle* out) {
+  if (!out) return set_error(FE_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  fe_handle h = new (std::nothrow) fe_equations_set();
+  if (!h) return set_error(FE_ERR_OUT_OF_MEMORY, "host allocation failed");
+  std::string msg;
+  int rc = cmfe::build_setup(desc, h->hs, msg);
+  if (rc) {
+    delete h;
+    return set_error(rc, msg);
+  }
+  auto fail = [&](int code) {
+    fe_destroy(h);
+    return code;
+  };
+  if (cudaGetDevice(&h->device) != cudaSuccess) return fail(set_error(FE_ERR_CUDA, "no CUDA device"));
+  if (cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess)
+    return fail(set_error(FE_ERR_CUDA, "cannot query the device"));
+  const auto& s = h->hs;
+  if ((rc = dev_upload(&h->d_elem_u, s.elem_u)) || (rc = dev_upload(&h->d_elem_p, s.elem_p)) ||
+      (rc = dev_upload(&h->d_row_ptr, s.row_ptr)) || (rc = dev_upload(&h->d_uu_row_ptr, s.uu_row_ptr)) ||
+      (rc = dev_upload(&h->d_cp_row_ptr, s.cp_row_ptr)) || (rc = dev_upload(&h->d_wu, s.wu)) ||
+      (rc = dev_upload(&h->d_wp, s.wp)) || (rc = dev_upload(&h->d_elem_table, s.elem_table)) ||
+      (rc = dev_upload(&h->d_colour_elems, s.colour_elems)) || (rc = dev_upload(&h->d_tables, s.tables)) ||
+      (rc = dev_upload(&h->d_geo, s.geo)) || (rc = dev_upload(&h->d_mat, s.mat)) ||
+      (rc = dev_upload(&h->d_gbf_u, s.gbf_u)) || (rc = dev_upload(&h->d_gbf_p, s.gbf_p)) ||
+      (rc = dev_upload(&h->d_gw, s.gw)))
+    return fail(rc);
+  if (cudaMalloc(&h->d_status, sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(h->d_status, 0, sizeof(unsigned)) != cudaSuccess)
+    return fail(set_error(FE_ERR_CUDA, "status allocation failed"));
+  *out = h;
+  return FE_NO_ERROR;
+}
+
+int fe_destroy(fe_handle h) {
+  if (!h) return FE_NO_ERROR;
+  void* ptrs[] = {h->d_elem_u, h->d_elem_p, h->d_row_ptr, h->d_uu_row_ptr, h->d_cp_row_ptr, h->d_wu,
+                  h->d_wp, h->d_elem_table, h->d_colour_elems, h->d_tables, h->d_geo, h->d_mat,
+                  h->d_gbf_u, h->d_gbf_p, h->d_gw, h->d_status, h->s_x, h->s_r, h->s_vals, h->s_cp,
+                  h->s_uu, h->s_elem};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete h;
+  return FE_NO_ERROR;
+}
+
+int fe_structure_calculate(const fe_mesh_desc* desc, int32_t base, int64_t* num_dofs, int64_t* nnz,
+                           int32_t* row_ptr, int32_t* col) {
+  if (base != 0 && base != 1) return set_error(FE_ERR_INVALID_ARGUMENT, "base must be 0 or 1");
+  HostSetup s;
+  std::string msg;
+  int rc = cmfe::build_setup(desc, s, msg);
+  if (rc) return set_error(rc, msg);
+  if (num_dofs) *num_dofs = s.ndofs;
+  if (nnz) *nnz = s.nnz;
+  if (row_ptr)
+    for (int64_t i = 0; i <= s.ndofs; ++i) row_ptr[i] = s.row_ptr[i] + base;
+  if (col)
+    for (int64_t i = 0; i < s.nnz; ++i) col[i] = s.col[i] + base;
+  return FE_NO_ERROR;
+}
+
+int fe_sizes(fe_handle h, int64_t* num_dofs, int64_t* nnz) {
+  if (!h) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL handle");
+  if (num_dofs) *num_dofs = h->hs.ndofs;
+  if (nnz) *nnz = h->hs.nnz;
+  return FE_NO_ERROR;
+}
+
+int fe_element_size(fe_handle h, int32_t* n) {
+  if (!h || !n) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL argument");
+  *n = h->hs.nrow;
+  return FE_NO_ERROR;
+}
+
+int fe_csr_pattern(fe_handle h, int32_t base, int32_t* row_ptr, int32_t* col) {
+  if (!h) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL handle");
+  if (base != 0 && base != 1) return set_error(FE_ERR_INVALID_ARGUMENT, "base must be 0 or 1");
+  const auto& s = h->hs;
+  if (row_ptr)
+    for (int64_t i = 0; i <= s.ndofs; ++i) row_ptr[i] = s.row_ptr[i] + base;
+  if (col)
+    for (int64_t i = 0; i < s.nnz; ++i) col[i] = s.col[i] + base;
+  return FE_NO_ERROR;
+}
+
+int fe_mixed_layout(fe_handle h, int64_t* nnz_uu, int64_t* nnz_coupling, int32_t* uu_row_ptr, int32_t* cp_row_ptr) {
+  if (!h) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL handle");
+  const auto& s = h->hs;
+  if (nnz_uu) *nnz_uu = s.nnz_uu;
+  if (nnz_coupling) *nnz_coupling = s.nnz_cp;
+  if (uu_row_ptr) std::memcpy(uu_row_ptr, s.uu_row_ptr.data(), s.uu_row_ptr.size() * sizeof(int32_t));
+  if (cp_row_ptr) std::memcpy(cp_row_ptr, s.cp_row_ptr.data(), s.cp_row_ptr.size() * sizeof(int32_t));
+  return FE_NO_ERROR;
+}
+
+int fe_residual_evaluate(fe_handle h, const double* x, double* r, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (!x || !r) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL x or r");
+  std::lock_guard<std::mutex> lk(h->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  bool hx;
+  const double* dx;
+  if ((rc = stage_in(h, x, &dx, st, &hx))) return rc;
+  const bool hr = !is_device_ptr(r);
+  double* dr = r;
+  if (hr) {
+    if ((rc = ensure((void**)&h->s_r, sizeof(double) * h->hs.ndofs))) return rc;
+    dr = h->s_r;
+  }
+  KParams kp = base_params(h);
+  kp.x = dx;
+  kp.r = dr;
+  if ((rc = run_colours<M_RES>(h, kp, st))) return rc;
+  if (hr) {
+    CUDA_TRY(cudaMemcpyAsync(r, dr, sizeof(double) * h->hs.ndofs, cudaMemcpyDeviceToHost, st));
+    return finish_status(h, st);
+  }
+  return FE_NO_ERROR;
+}
+
+int fe_jacobian_evaluate(fe_handle h, const double* x, double* values, double* r, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (!x || !values) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL x or values");
+  std::lock_guard<std::mutex> lk(h->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  bool hx;
+  const double* dx;
+  if ((rc = stage_in(h, x, &dx, st, &hx))) return rc;
+  const bool hv = !is_device_ptr(values);
+  const bool hr = r && !is_device_ptr(r);
+  double* dv = values;
+  double* dr = r;
+  if (hv) {
+    if ((rc = ensure((void**)&h->s_vals, sizeof(double) * h->hs.nnz))) return rc;
+    dv = h->s_vals;
+  }
+  if (hr) {
+    if ((rc = ensure((void**)&h->s_r, sizeof(double) * h->hs.ndofs))) return rc;
+    dr = h->s_r;
+  }
+  KParams kp = base_params(h);
+  kp.x = dx;
+  kp.vals = dv;
+  kp.r = dr;
+  if ((rc = run_colours<M_JAC>(h, kp, st))) return rc;
+  if (hv) CUDA_TRY(cudaMemcpyAsync(values, dv, sizeof(double) * h->hs.nnz, cudaMemcpyDeviceToHost, st));
+  if (hr) CUDA_TRY(cudaMemcpyAsync(r, dr, sizeof(double) * h->hs.ndofs, cudaMemcpyDeviceToHost, st));
+  if (hv || hr) return finish_status(h, st);
+  return FE_NO_ERROR;
+}
+
+int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, double* values_coupling, double* r,
+                               void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (!x || !values_uu || !values_coupling) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL argument");
+  std::lock_guard<std::mutex> lk(h->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  bool hx;
+  const double* dx;
+  if ((rc = stage_in(h, x, &dx, st, &hx))) return rc;
+  const bool hu = !is_device_ptr(values_uu), hc = !is_device_ptr(values_coupling);
+  const bool hr = r && !is_device_ptr(r);
+  float* du = values_uu;
+  double* dc = values_coupling;
+  double* dr = r;
+  if (hu) {
+    if ((rc = ensure((void**)&h->s_uu, sizeof(float) * h->hs.nnz_uu))) return rc;
+    du = h->s_uu;
+  }
+  if (hc) {
+    if ((rc = ensure((void**)&h->s_cp, sizeof(double) * h->hs.nnz_cp))) return rc;
+    dc = h->s_cp;
+  }
+  if (hr) {
+    if ((rc = ensure((void**)&h->s_r, sizeof(double) * h->hs.ndofs))) return rc;
+    dr = h->s_r;
+  }
+  KParams kp = base_params(h);
+  kp.x = dx;
+  kp.vals_uu = du;
+  kp.vals = dc;
+  kp.r = dr;
+  if ((rc = run_colours<M_MIX>(h, kp, st))) return rc;
+  if (hu) CUDA_TRY(cudaMemcpyAsync(values_uu, du, sizeof(float) * h->hs.nnz_uu, cudaMemcpyDeviceToHost, st));
+  if (hc) CUDA_TRY(cudaMemcpyAsync(values_coupling, dc, sizeof(double) * h->hs.nnz_cp, cudaMemcpyDeviceToHost, st));
+  if (hr) CUDA_TRY(cudaMemcpyAsync(r, dr, sizeof(double) * h->hs.ndofs, cudaMemcpyDeviceToHost, st));
+  if (hu || hc || hr) return finish_status(h, st);
+  return FE_NO_ERROR;
+}
+
+static int element_eval(fe_handle h, const double* x, int32_t first, int32_t count, double* out, void* stream,
+                        bool jac) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (!x || !out || first < 0 || count < 0 || (int64_t)first + count > h->hs.ne)
+    return set_error(FE_ERR_INVALID_ARGUMENT, "invalid element range or NULL pointer");
+  if (count == 0) return FE_NO_ERROR;
+  std::lock_guard<std::mutex> lk(h->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  bool hx;
+  const double* dx;
+  if ((rc = stage_in(h, x, &dx, st, &hx))) return rc;
+  const size_t n = (size_t)h->hs.nrow;
+  const size_t bytes = sizeof(double) * (size_t)count * (jac ? n * n : n);
+  const bool ho = !is_device_ptr(out);
+  double* dout = out;
+  if (ho) {
+    if (h->s_elem_bytes < bytes) {
+      if (h->s_elem) cudaFree(h->s_elem);
+      h->s_elem = nullptr;
+      h->s_elem_bytes = 0;
+      if ((rc = ensure((void**)&h->s_elem, bytes))) return rc;
+      h->s_elem_bytes = bytes;
+    }
+    dout = h->s_elem;
+  }
+  KParams kp = base_params(h);
+  kp.x = dx;
+  kp.elem_out = dout;
+  kp.first_elem = first;
+  kp.count = count;
+  kp.elems = nullptr;
+  if ((rc = jac ? launch<M_EJAC>(h, kp, st) : launch<M_ERES>(h, kp, st))) return rc;
+  if (ho) {
+    CUDA_TRY(cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, st));
+    return finish_status(h, st);
+  }
+  return FE_NO_ERROR;
+}
+
+int fe_element_residuals(fe_handle h, const double* x, int32_t first, int32_t count, double* out, void* stream) {
+  return element_eval(h, x, first, count, out, stream, false);
+}
+
+int fe_element_jacobians(fe_handle h, const double* x, int32_t first, int32_t count, double* out, void* stream) {
+  return element_eval(h, x, first, count, out, stream, true);
+}
+
+int fe_check(fe_handle h, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(h->mu);
+  return finish_status(h, (cudaStream_t)stream);
+}
+
+int fe_launch_count(fe_handle h, int64_t* count) {
+  if (!h || !count) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL argument");
+  *count = h->launches;
+  return FE_NO_ERROR;
+}
+
+}  // extern "C"

@@ -1,0 +1,191 @@
+"""Host-side mirror of the reference's finite-elasticity equations-set call
+surface for the assembly path, on top of the C ABI (include/cm_fe.h).
+
+Reference call surface mirrored (OpenCMISS-Iron):
+  * EQUATIONS_SET_RESIDUAL_EVALUATE (equations_set_routines.f90:5184) ->
+    :meth:`FiniteElasticityEquationsSet.residual_evaluate`
+  * EQUATIONS_SET_JACOBIAN_EVALUATE (:4694) ->
+    :meth:`FiniteElasticityEquationsSet.jacobian_evaluate`
+  * FiniteElasticity_FiniteElement{Residual,Jacobian}Evaluate
+    (finite_elasticity_routines.f90:1260, :842) ->
+    :meth:`element_residuals`, :meth:`element_jacobians`
+  * the Jacobian's CSR structure (JacobianMatrix_StructureCalculate,
+    equations_matrices_routines.f90:5048) -> :meth:`csr_pattern`
+
+Arrays may be numpy arrays (host memory: the call copies in and out and
+returns when done) or CUDA torch tensors (device memory: the call is
+asynchronous on the current torch stream).  Failures raise
+:class:`cm_gb300._lib.FEError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import FEError, check  # noqa: F401
+from .mesh import Mesh
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return a.ctypes.data
+    # torch tensor
+    if not a.is_contiguous():
+        raise ValueError("tensor must be contiguous")
+    return a.data_ptr()
+
+
+def _stream(a):
+    if isinstance(a, np.ndarray) or a is None:
+        return None
+    import torch
+    return C.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
+
+
+class FiniteElasticityEquationsSet:
+    """One finite-elasticity equations set (mesh + law + materials) on the
+    current CUDA device."""
+
+    def __init__(self, mesh: Mesh):
+        self.mesh = mesh
+        L = _lib.load()
+        self._keep = []
+
+        def arr(a, dt):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=dt)
+            self._keep.append(a)
+            return a.ctypes.data
+
+        mats = np.asarray(mesh.materials, dtype=np.float64)
+        d = _lib.FEMeshDesc()
+        d.num_elements = mesh.ne
+        d.num_nodes_u = mesh.nu
+        d.num_nodes_p = mesh.np
+        d.nodes_per_xi_u = mesh.nxi_u
+        d.pressure_interpolation = mesh.p_mode
+        d.law = mesh.law
+        d.num_material_components = mats.shape[-1]
+        d.materials_per_element = 1 if mats.ndim == 2 else 0
+        d.element_nodes_u = arr(mesh.elem_u, np.int32)
+        d.element_nodes_p = arr(mesh.elem_p, np.int32)
+        d.geometry = arr(mesh.X, np.float64)
+        d.materials = arr(mats, np.float64)
+        d.fibre_angles = arr(mesh.fibre, np.float64)
+        h = C.c_void_p()
+        check(L.fe_create(C.byref(d), C.byref(h)))
+        self._keep = []
+        self._h = h
+        nd, nnz = C.c_int64(), C.c_int64()
+        check(L.fe_sizes(h, C.byref(nd), C.byref(nnz)))
+        self.ndofs, self.nnz = nd.value, nnz.value
+        n = C.c_int32()
+        check(L.fe_element_size(h, C.byref(n)))
+        self.element_size = n.value
+        nuu, ncp = C.c_int64(), C.c_int64()
+        check(L.fe_mixed_layout(h, C.byref(nuu), C.byref(ncp), None, None))
+        self.nnz_uu, self.nnz_coupling = nuu.value, ncp.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().fe_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -------------------------------------------------------------- pattern
+    def csr_pattern(self, base: int = 0):
+        rp = np.zeros(self.ndofs + 1, dtype=np.int32)
+        col = np.zeros(self.nnz, dtype=np.int32)
+        check(_lib.load().fe_csr_pattern(self._h, base, rp.ctypes.data, col.ctypes.data))
+        return rp, col
+
+    def mixed_layout(self):
+        uu = np.zeros(3 * self.mesh.nu + 1, dtype=np.int32)
+        cp = np.zeros(self.ndofs + 1, dtype=np.int32)
+        check(_lib.load().fe_mixed_layout(self._h, None, None, uu.ctypes.data, cp.ctypes.data))
+        return uu, cp
+
+    # ----------------------------------------------------------- evaluation
+    def _alloc_like(self, x, n, dtype):
+        if isinstance(x, np.ndarray):
+            return np.zeros(n, dtype=dtype)
+        import torch
+        return torch.empty(n, dtype={np.float64: torch.float64, np.float32: torch.float32}[dtype], device=x.device)
+
+    def residual_evaluate(self, x, r=None):
+        r = self._alloc_like(x, self.ndofs, np.float64) if r is None else r
+        check(_lib.load().fe_residual_evaluate(self._h, _ptr(x), _ptr(r), _stream(x)))
+        return r
+
+    def jacobian_evaluate(self, x, values=None, r=None):
+        values = self._alloc_like(x, self.nnz, np.float64) if values is None else values
+        check(_lib.load().fe_jacobian_evaluate(self._h, _ptr(x), _ptr(values), _ptr(r), _stream(x)))
+        return values
+
+    def jacobian_evaluate_mixed(self, x, values_uu=None, values_coupling=None, r=None):
+        values_uu = self._alloc_like(x, self.nnz_uu, np.float32) if values_uu is None else values_uu
+        values_coupling = (self._alloc_like(x, self.nnz_coupling, np.float64)
+                           if values_coupling is None else values_coupling)
+        check(_lib.load().fe_jacobian_evaluate_mixed(self._h, _ptr(x), _ptr(values_uu), _ptr(values_coupling),
+                                                     _ptr(r), _stream(x)))
+        return values_uu, values_coupling
+
+    def element_residuals(self, x, first=0, count=None):
+        count = self.mesh.ne - first if count is None else count
+        out = self._alloc_like(x, count * self.element_size, np.float64)
+        check(_lib.load().fe_element_residuals(self._h, _ptr(x), first, count, _ptr(out), _stream(x)))
+        return out.reshape(count, self.element_size)
+
+    def element_jacobians(self, x, first=0, count=None):
+        """Element Jacobians as (count, row, col) arrays (the C ABI writes
+        them column-major, like ELEMENT_JACOBIAN%MATRIX)."""
+        count = self.mesh.ne - first if count is None else count
+        n = self.element_size
+        out = self._alloc_like(x, count * n * n, np.float64)
+        check(_lib.load().fe_element_jacobians(self._h, _ptr(x), first, count, _ptr(out), _stream(x)))
+        return out.reshape(count, n, n).transpose(1, 2) if not isinstance(out, np.ndarray) else \
+            out.reshape(count, n, n).transpose(0, 2, 1)
+
+    def check_status(self, x=None):
+        check(_lib.load().fe_check(self._h, _stream(x)))
+
+    def launch_count(self):
+        c = C.c_int64()
+        check(_lib.load().fe_launch_count(self._h, C.byref(c)))
+        return c.value
+
+    # ------------------------------------------------------------- helpers
+    def mixed_to_full(self, values_uu, values_coupling):
+        """Merges the mixed split back into one FP64 array in pattern order
+        (host numpy; for checking)."""
+        uu_rp, cp_rp = self.mixed_layout()
+        rp, _ = self.csr_pattern()
+        vu = np.asarray(values_uu, dtype=np.float64)
+        vc = np.asarray(values_coupling, dtype=np.float64)
+        out = np.empty(self.nnz)
+        nu3 = 3 * self.mesh.nu
+        for r in range(self.ndofs):
+            a, b = rp[r], rp[r + 1]
+            if r < nu3:
+                k = uu_rp[r + 1] - uu_rp[r]
+                out[a:a + k] = vu[uu_rp[r]:uu_rp[r + 1]]
+                out[a + k:b] = vc[cp_rp[r]:cp_rp[r + 1]]
+            else:
+                out[a:b] = vc[cp_rp[r]:cp_rp[r + 1]]
+        return out

@@ -1,0 +1,164 @@
+/*
+ * cm_fe.h — C ABI of the GB300 finite-elasticity assembly library
+ * (libcm_fe.so).
+ *
+ * The library replaces the per-element hot loop of OpenCMISS-Iron's static
+ * nonlinear finite-element assembly for incompressible Mooney-Rivlin and
+ * transversely-isotropic Guccione elasticity: the element residual and
+ * Jacobian with Gauss-point constitutive stress, and their addition into the
+ * compressed-row (CSR) Jacobian and the residual vector.  The assembled
+ * system is handed unchanged to the caller's Newton/linear solver.
+ *
+ * Conventions (mirroring the reference's generated C bindings,
+ * bindings/generate_bindings/c.py:31-40 and :165-225):
+ *   - every entry point returns an int status: FE_NO_ERROR (0) on success,
+ *     a negative FE_ERR_* code otherwise; fe_last_error() returns the text;
+ *   - objects are opaque handles; arrays are (pointer, size) pairs of plain
+ *     C types; no entry point aborts the process;
+ *   - degrees of freedom are numbered like the reference's dependent field
+ *     on one rank (field_routines.f90:10354-10540, "separated component" dof
+ *     order): u_x of all u nodes, u_y, u_z, then the hydrostatic pressure
+ *     (one per element for element-based pressure, else one per pressure
+ *     node).  The dependent field holds the deformed position z (the
+ *     reference initialises it from the geometric field), not a displacement.
+ *   - dof, residual and matrix-value arrays may live in host memory or in
+ *     device memory of the current CUDA device; the library detects which.
+ *     Calls given host memory copy through pinned staging buffers and return
+ *     after the result is back in host memory; calls given device memory are
+ *     asynchronous on the given stream (NULL = legacy default stream).
+ */
+#ifndef CM_FE_H
+#define CM_FE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define FE_NO_ERROR 0
+#define FE_ERR_INVALID_ARGUMENT (-1)
+#define FE_ERR_CUDA (-2)
+#define FE_ERR_OUT_OF_MEMORY (-3)
+#define FE_ERR_NOT_SUPPORTED (-4)
+#define FE_ERR_NUMERICAL (-5) /* a Gauss point had det F <= 0 or a non-finite value */
+#define FE_ERR_PATTERN (-6)   /* an element entry has no slot in the CSR pattern */
+
+/* Constitutive laws: the reference's equations-set subtypes
+ * (equations_set_constants.f90:121, :135). */
+#define FE_LAW_MOONEY_RIVLIN 1
+#define FE_LAW_GUCCIONE 15
+
+/* Interpolation of the hydrostatic-pressure component. */
+#define FE_PRESSURE_ELEMENT_BASED 0 /* one constant per element */
+#define FE_PRESSURE_NODE_BASED 1    /* trilinear Lagrange on its own nodes */
+
+/* Mesh and equations-set description.  The geometric field, the fibre field
+ * and the three displacement components share mesh component 1 (tensor-product
+ * Lagrange, 2 or 3 nodes per xi direction); a node-based pressure uses a
+ * trilinear mesh component.  Element node order is xi1 fastest, then xi2,
+ * then xi3 (BASIS_LHTP node numbering, basis_routines.f90:2251-2374). */
+typedef struct fe_mesh_desc {
+  int32_t num_elements;
+  int32_t num_nodes_u;         /* nodes of mesh component 1 */
+  int32_t num_nodes_p;         /* pressure nodes; 0 for element-based pressure */
+  int32_t nodes_per_xi_u;      /* 2 trilinear, 3 triquadratic */
+  int32_t pressure_interpolation; /* FE_PRESSURE_* */
+  int32_t law;                 /* FE_LAW_* */
+  int32_t num_material_components; /* 2 (c1, c2) for MR; 4 (C, bf, bt, bfs) for Guccione */
+  int32_t materials_per_element;   /* 0: one set for all elements; 1: one set per element */
+  const int32_t* element_nodes_u;  /* [num_elements][nodes_per_xi_u^3], 0-based */
+  const int32_t* element_nodes_p;  /* [num_elements][8], 0-based; NULL if element-based */
+  const double* geometry;          /* [3][num_nodes_u], component-major */
+  const double* materials;         /* [num_material_components] or [num_elements][..] */
+  const double* fibre_angles;      /* NULL, or [3][num_nodes_u] fibre/imbrication/sheet (radians) */
+} fe_mesh_desc;
+
+typedef struct fe_equations_set* fe_handle;
+
+/* Equations-set set-up: validates the mesh, numbers the dofs, builds the
+ * Jacobian's CSR sparsity pattern (JacobianMatrix_StructureCalculate,
+ * equations_matrices_routines.f90:5048-5340), the element colouring used for
+ * the deterministic scatter, and the device-resident geometric Gauss-point
+ * data.  Replaces EQUATIONS_MATRICES_CREATE_FINISH (:403) for this path. */
+int fe_create(const fe_mesh_desc* desc, fe_handle* out);
+int fe_destroy(fe_handle h);
+
+/* Host-only structure calculation (no device needed): the CSR pattern the
+ * set-up of fe_create builds for this mesh (JacobianMatrix_StructureCalculate,
+ * equations_matrices_routines.f90:5048-5340).  num_dofs and nnz are always
+ * returned; row_ptr (num_dofs+1) and col (nnz) are filled when not NULL, with
+ * 1-based (base = 1, as ROW_INDICES/COLUMN_INDICES) or 0-based indices. */
+int fe_structure_calculate(const fe_mesh_desc* desc, int32_t base, int64_t* num_dofs, int64_t* nnz,
+                           int32_t* row_ptr, int32_t* col);
+
+/* Sizes: number of dofs (= rows = columns) and number of CSR nonzeros. */
+int fe_sizes(fe_handle h, int64_t* num_dofs, int64_t* nnz);
+
+/* Copy the CSR pattern out (host arrays).  base = 1 gives the reference's
+ * 1-based ROW_INDICES / COLUMN_INDICES (matrix_vector.f90, MATRIX_TYPE
+ * types.f90:858-877); base = 0 gives 0-based indices.  row_ptr has
+ * num_dofs+1 entries, col has nnz entries. */
+int fe_csr_pattern(fe_handle h, int32_t base, int32_t* row_ptr, int32_t* col);
+
+/* Residual evaluation: r = assembled element residuals at dof vector x
+ * (EQUATIONS_SET_RESIDUAL_EVALUATE_STATIC_FEM, equations_set_routines.f90:
+ * 5483-5640, with FiniteElasticity_FiniteElementResidualEvaluate,
+ * finite_elasticity_routines.f90:1260-1639, and EQUATIONS_MATRICES_ELEMENT_ADD,
+ * equations_matrices_routines.f90:1259-1395).  FP64.  r is overwritten. */
+int fe_residual_evaluate(fe_handle h, const double* x, double* r, void* stream);
+
+/* Jacobian evaluation in FP64: CSR values (nnz, in pattern order) of the
+ * assembled Jacobian at x (EQUATIONS_SET_JACOBIAN_EVALUATE_STATIC_FEM,
+ * equations_set_routines.f90:4878-5024, with
+ * FiniteElasticity_FiniteElementJacobianEvaluate,
+ * finite_elasticity_routines.f90:842-1175, and
+ * EQUATIONS_MATRICES_JACOBIAN_ELEMENT_ADD, equations_matrices_routines.f90:
+ * 3174-3225).  values is overwritten.  If r is not NULL the residual at x is
+ * produced by the same pass. */
+int fe_jacobian_evaluate(fe_handle h, const double* x, double* values, double* r, void* stream);
+
+/* Mixed-precision Jacobian: the displacement-displacement block in FP32, the
+ * displacement-pressure coupling blocks (and the structurally zero
+ * pressure-pressure block) in FP64.  The two value arrays follow the split
+ * pattern returned by fe_mixed_layout().  If r is not NULL the FP64 residual
+ * at x is produced by the same pass.  No counterpart in the reference (which
+ * assembles in FP64 only); its FP64 parts match fe_jacobian_evaluate. */
+int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, double* values_coupling,
+                               double* r, void* stream);
+
+/* Split layout of the mixed Jacobian.  Rows of displacement dofs keep their
+ * displacement columns in values_uu (uu_row_ptr over the 3*num_nodes_u u rows)
+ * and their pressure columns in values_coupling; rows of pressure dofs keep
+ * all their columns in values_coupling.  cp_row_ptr has num_dofs+1 entries.
+ * Both arrays are 0-based host arrays; either may be NULL. */
+int fe_mixed_layout(fe_handle h, int64_t* nnz_uu, int64_t* nnz_coupling, int32_t* uu_row_ptr,
+                    int32_t* cp_row_ptr);
+
+/* Element-level evaluation for a contiguous range of elements (0-based), the
+ * direct counterparts of FiniteElasticity_FiniteElementResidualEvaluate /
+ * ..JacobianEvaluate(EQUATIONS_SET, ELEMENT_NUMBER).  Element matrices are
+ * written column-major (ELEMENT_JACOBIAN%MATRIX(row, col)), n x n each with
+ * n = fe_element_size(); element vectors n each. */
+int fe_element_size(fe_handle h, int32_t* n);
+int fe_element_residuals(fe_handle h, const double* x, int32_t first, int32_t count, double* out, void* stream);
+int fe_element_jacobians(fe_handle h, const double* x, int32_t first, int32_t count, double* out, void* stream);
+
+/* Waits for the handle's work on `stream` and reports numerical problems
+ * seen by the kernels since the last call (FE_ERR_NUMERICAL) — the device
+ * counterpart of the reference's error flags, set instead of trapping. */
+int fe_check(fe_handle h, void* stream);
+
+/* Number of kernels launched by the library since the handle was created. */
+int fe_launch_count(fe_handle h, int64_t* count);
+
+/* Copies the text of the last error of the calling thread into buf
+ * (cmfe_ExtractErrorMessage, bindings/python/opencmiss/_iron_utils.py:77). */
+int fe_last_error(char* buf, int32_t size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CM_FE_H */

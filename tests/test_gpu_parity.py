@@ -1,0 +1,221 @@
+"""GPU parity tests: the CUDA path through the C ABI against the FP64 oracle.
+
+Tolerance (FP64 path, per entry): |gpu - oracle| <= 1e-12 |oracle| + 1e-13 S,
+where S is the largest magnitude of the element matrix / vector (element
+level) or of the assembled array (global level).  The absolute floor covers
+entries that cancel to (near) zero, whose rounding noise is set by the size
+of the terms, not by the entry.  The CSR pattern must match bit for bit.
+The FP32 block of the mixed path is checked at 2e-5 relative to S.
+"""
+import numpy as np
+import pytest
+
+from cm_gb300 import FEError, FiniteElasticityEquationsSet, _lib
+from cm_gb300 import mesh as M
+
+pytestmark = pytest.mark.gpu
+
+REL, FLOOR = 1e-12, 1e-13
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as _torch
+    if not _torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    _lib.load()
+    return _torch
+
+
+def assert_entrywise(gpu, ref, rel=REL, floor=FLOOR, scale=None, what=""):
+    gpu = np.asarray(gpu, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    assert gpu.shape == ref.shape, what
+    S = np.abs(ref).max() if scale is None else scale
+    err = np.abs(gpu - ref)
+    bound = rel * np.abs(ref) + floor * S
+    bad = err > bound
+    assert not bad.any(), "%s: %d entries off, worst %.3e (bound %.3e, scale %.3e)" % (
+        what, bad.sum(), err.max(), bound[np.argmax(err - bound)], S)
+
+
+def meshes():
+    return {
+        "cfg1_lin_elem_mr": M.regular_box(4, 4, 4, nxi_u=2, pressure="element", law=M.MR, materials=(2.0, 6.0)),
+        "quad_node_mr_perturbed": M.regular_box(3, 2, 2, nxi_u=3, pressure="node", law=M.MR,
+                                                materials=(2.0, 6.0), perturb=0.1, seed=7),
+        "quad_node_guccione_fibres": M.regular_box(2, 2, 2, lengths=(4.0, 4.0, 1.0), nxi_u=3, pressure="node",
+                                                   law=M.GUCCIONE, materials=(0.88, 18.5, 3.58, 1.63),
+                                                   fibre=np.array([[0.4], [0.1], [-0.3]]), perturb=0.05, seed=9),
+        "lin_node_mr": M.regular_box(3, 3, 2, nxi_u=2, pressure="node", law=M.MR, materials=(1.0, 3.0)),
+        "quad_elem_mr": M.regular_box(2, 1, 2, nxi_u=3, pressure="element", law=M.MR, materials=(0.5, 9.0)),
+    }
+
+
+def state(m, seed=3):
+    return M.deformed_state(m, stretch=1.07, shear=0.05, noise=0.04, pressure=-2.0, seed=seed)
+
+
+@pytest.mark.parametrize("name", list(meshes()))
+def test_element_parity(torch, oracle, name):
+    m = meshes()[name]
+    x = state(m)
+    es = FiniteElasticityEquationsSet(m)
+    P = oracle.Problem(m)
+    xd = torch.from_numpy(x).cuda()
+    K = es.element_jacobians(xd).cpu().numpy()
+    R = es.element_residuals(xd).cpu().numpy()
+    es.check_status(xd)
+    for e in range(m.ne):
+        Ko = P.element_jacobian(e, x)
+        Ro = P.element_residual(e, x)
+        assert_entrywise(K[e], Ko, what="%s K_e[%d]" % (name, e))
+        assert_entrywise(R[e], Ro, what="%s r_e[%d]" % (name, e))
+
+
+@pytest.mark.parametrize("name", list(meshes()))
+def test_assembled_parity_and_pattern(torch, oracle, name):
+    m = meshes()[name]
+    x = state(m)
+    es = FiniteElasticityEquationsSet(m)
+    P = oracle.Problem(m)
+    rp_o, col_o = P.pattern()
+    rp, col = es.csr_pattern(base=1)
+    assert np.array_equal(rp, rp_o) and np.array_equal(col, col_o)
+    vo, ro = P.assemble(x, rp_o, col_o, nthreads=1)
+    xd = torch.from_numpy(x).cuda()
+    r = torch.empty_like(xd)
+    v = es.jacobian_evaluate(xd, r=r)
+    r2 = es.residual_evaluate(xd)
+    es.check_status(xd)
+    assert_entrywise(v.cpu().numpy(), vo, what=name + " CSR values")
+    assert_entrywise(r.cpu().numpy(), ro, what=name + " residual (Jacobian pass)")
+    assert_entrywise(r2.cpu().numpy(), ro, what=name + " residual")
+
+
+def test_host_and_device_pointers_agree(torch):
+    m = meshes()["quad_node_mr_perturbed"]
+    x = state(m)
+    es = FiniteElasticityEquationsSet(m)
+    vh = es.jacobian_evaluate(x)                 # numpy in, numpy out
+    rh = es.residual_evaluate(x)
+    xd = torch.from_numpy(x).cuda()
+    vd = es.jacobian_evaluate(xd).cpu().numpy()
+    rd = es.residual_evaluate(xd).cpu().numpy()
+    assert np.array_equal(vh, vd) and np.array_equal(rh, rd)
+
+
+def test_deterministic(torch):
+    m = M.regular_box(6, 5, 4, nxi_u=3, pressure="node", perturb=0.1, seed=1)
+    x = torch.from_numpy(state(m)).cuda()
+    es = FiniteElasticityEquationsSet(m)
+    a = es.jacobian_evaluate(x).clone()
+    b = es.jacobian_evaluate(x).clone()
+    assert torch.equal(a, b)
+    ua, ca = es.jacobian_evaluate_mixed(x)
+    ua, ca = ua.clone(), ca.clone()
+    ub, cb = es.jacobian_evaluate_mixed(x)
+    assert torch.equal(ua, ub) and torch.equal(ca, cb)
+
+
+@pytest.mark.parametrize("name", ["quad_node_mr_perturbed", "cfg1_lin_elem_mr", "quad_node_guccione_fibres"])
+def test_mixed_precision(torch, name):
+    m = meshes()[name]
+    x = torch.from_numpy(state(m)).cuda()
+    es = FiniteElasticityEquationsSet(m)
+    r64 = torch.empty_like(x)
+    v64 = es.jacobian_evaluate(x, r=r64).cpu().numpy()
+    rm = torch.empty_like(x)
+    vu, vc = es.jacobian_evaluate_mixed(x, r=rm)
+    es.check_status(x)
+    full = es.mixed_to_full(vu.cpu().numpy(), vc.cpu().numpy())
+    uu_rp, cp_rp = es.mixed_layout()
+    rp, _ = es.csr_pattern()
+    is_uu = np.zeros(es.nnz, dtype=bool)
+    for r in range(3 * m.nu):
+        is_uu[rp[r]:rp[r] + (uu_rp[r + 1] - uu_rp[r])] = True
+    # FP64 parts: identical arithmetic to the FP64 path
+    assert np.array_equal(full[~is_uu], v64[~is_uu])
+    assert torch.equal(rm, r64)
+    # FP32 tangent block
+    S = np.abs(v64).max()
+    assert np.abs(full[is_uu] - v64[is_uu]).max() < 2e-5 * S
+
+
+def test_inverted_element_reports_numerical_error(torch):
+    """A host-made fault: an element turned inside out gives FE_ERR_NUMERICAL
+    (the kernel flags it, it does not trap)."""
+    m = M.regular_box(2, 2, 2, nxi_u=2, pressure="element")
+    x = state(m)
+    nu = m.nu
+    n0 = m.elem_u[0, 0]
+    x[n0] += 3.0 * m.lengths[0] / m.dims[0]  # push a corner through the element
+    es = FiniteElasticityEquationsSet(m)
+    with pytest.raises(FEError) as ei:
+        es.residual_evaluate(x)
+    assert ei.value.code == _lib.FE_ERR_NUMERICAL
+    # the context stays usable
+    r = es.residual_evaluate(state(m))
+    assert np.isfinite(r).all()
+    assert nu > 0
+
+
+def _csr_matvec(torch, rp, col, vals, v):
+    n = rp.numel() - 1
+    rows = torch.repeat_interleave(torch.arange(n, device=v.device), rp[1:] - rp[:-1])
+    y = torch.zeros(n, dtype=torch.float64, device=v.device)
+    y.index_add_(0, rows, vals.to(torch.float64) * v[col.long()])
+    return y
+
+
+def test_full_size_config2_properties(torch, oracle):
+    """32^3 triquadratic / trilinear-pressure box (824k u dofs, 178.7M nnz):
+    size-independent checks of the FP64 and mixed paths — element-sampled
+    parity against the oracle, symmetry u^T J v = v^T J u, and J v against a
+    central difference of the residual."""
+    m = M.regular_box(32, 32, 32, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0), perturb=0.1, seed=2)
+    x = M.deformed_state(m, stretch=1.1, shear=0.05, noise=0.02, pressure=-2.0, seed=4)
+    es = FiniteElasticityEquationsSet(m)
+    assert es.nnz == 178723696 and es.ndofs == 859812
+    xd = torch.from_numpy(x).cuda()
+    sample = [0, 1, 777, 16383, 20000, m.ne - 1]
+    P = oracle.Problem(m)
+    for e in sample:
+        Ke = es.element_jacobians(xd, e, 1).cpu().numpy()[0]
+        assert_entrywise(Ke, P.element_jacobian(e, x), what="cfg2 K_e[%d]" % e)
+    rp, col = es.csr_pattern()
+    rp_d = torch.from_numpy(rp.astype(np.int64)).cuda()
+    col_d = torch.from_numpy(col).cuda()
+    r = torch.empty_like(xd)
+    vals = es.jacobian_evaluate(xd, r=r)
+    es.check_status(xd)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    u = torch.randn(es.ndofs, dtype=torch.float64, device="cuda", generator=g)
+    v = torch.randn(es.ndofs, dtype=torch.float64, device="cuda", generator=g)
+    Jv = _csr_matvec(torch, rp_d, col_d, vals, v)
+    Ju = _csr_matvec(torch, rp_d, col_d, vals, u)
+    a, b = float(u @ Jv), float(v @ Ju)
+    assert abs(a - b) <= 1e-10 * (abs(a) + 1e-30)
+    h = 1e-6
+    rp_ = es.residual_evaluate(xd + h * v)
+    rm_ = es.residual_evaluate(xd - h * v)
+    fd = (rp_ - rm_) / (2 * h)
+    assert float((fd - Jv).norm() / Jv.norm()) < 1e-6
+    # mixed path on the same state
+    vu, vc = es.jacobian_evaluate_mixed(xd)
+    uu_rp, cp_rp = es.mixed_layout()
+    nu3 = 3 * m.nu
+    uu_idx = np.concatenate([np.arange(rp[i], rp[i] + uu_rp[i + 1] - uu_rp[i]) for i in range(0, nu3, 997)])
+    uu_pos = np.concatenate([np.arange(uu_rp[i], uu_rp[i + 1]) for i in range(0, nu3, 997)])
+    d64 = vals[torch.from_numpy(uu_idx).cuda()]
+    d32 = vu[torch.from_numpy(uu_pos).cuda()].double()
+    assert float((d64 - d32).abs().max()) < 2e-5 * float(vals.abs().max())
+
+
+def test_native_library_launches(torch):
+    m = meshes()["cfg1_lin_elem_mr"]
+    es = FiniteElasticityEquationsSet(m)
+    before = es.launch_count()
+    es.jacobian_evaluate(torch.from_numpy(state(m)).cuda())
+    torch.cuda.synchronize()
+    assert es.launch_count() - before >= 8  # one launch per element colour

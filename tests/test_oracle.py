@@ -1,0 +1,252 @@
+"""CPU tests: pin the oracle with the reference's own known answers and
+closed forms, and check the product's host-side logic against it.
+
+Known answers used (the reference ships no golden vectors for this path):
+  * Gauss-Legendre self-check, basis_routines.f90:5886-5895
+  * finite-difference element Jacobian rule, equations_set_routines.f90:
+    3086-3130 (delta = (1+||x||_2)*1e-7)
+  * homogeneous uniaxial stretch of incompressible Mooney-Rivlin with the
+    reference's sigma = dev(sigma_bar) + p I split
+    (finite_elasticity_routines.f90:4386-4414)
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from cm_gb300 import mesh as M
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def small_meshes():
+    return [
+        ("lin_elem", M.regular_box(2, 2, 2, nxi_u=2, pressure="element", law=M.MR, materials=(2.0, 6.0))),
+        ("quad_node", M.regular_box(2, 2, 2, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0),
+                                    perturb=0.1, seed=3)),
+        ("quad_node_guccione", M.regular_box(2, 2, 1, lengths=(4.0, 4.0, 1.0), nxi_u=3, pressure="node",
+                                             law=M.GUCCIONE, materials=(0.88, 18.5, 3.58, 1.63),
+                                             fibre=np.array([[0.3], [0.1], [-0.2]]), perturb=0.05, seed=5)),
+    ]
+
+
+def test_gauss_legendre_self_check(oracle):
+    # basis_routines.f90:5886-5895: integrate y = x + 1 over [0, 1]
+    _, w, xi = oracle.basis_tables(2)
+    x1 = xi[:3, 0]
+    w1 = w[:3] / (w[0] / (2.5 / 9.0))  # recover the 1-D weights of the first xi line
+    t1 = np.sum((x1 + 1.0) * w1)
+    assert abs(t1 - 1.5) < 1e-15
+    # 3-point rule on [0,1]^3 integrates every monomial of degree <= 5 per direction exactly
+    for p in range(6):
+        for q in range(6):
+            val = np.sum(w * xi[:, 0] ** p * xi[:, 1] ** q)
+            assert abs(val - 1.0 / ((p + 1) * (q + 1))) < 1e-14
+    assert abs(w.sum() - 1.0) < 1e-15
+
+
+@pytest.mark.parametrize("nxi", [2, 3])
+def test_basis_partition_of_unity(oracle, nxi):
+    g, _, _ = oracle.basis_tables(nxi)
+    assert np.allclose(g[:, 0, :].sum(axis=1), 1.0, atol=1e-15)
+    assert np.allclose(g[:, 1:, :].sum(axis=2), 0.0, atol=1e-13)
+
+
+@pytest.mark.parametrize("dims", [(2, 3, 4), (4, 4, 4), (1, 2, 1)])
+@pytest.mark.parametrize("nxi,pmode", [(2, "element"), (3, "node"), (2, "node")])
+def test_mesh_numbering_matches_reference_restatement(oracle, dims, nxi, pmode):
+    m = M.regular_box(*dims, nxi_u=nxi, pressure=pmode)
+    eu, ep, npn = oracle.regular_mesh(*dims, nxi, pmode == "node")
+    assert np.array_equal(m.elem_u, eu)
+    if pmode == "node":
+        assert np.array_equal(m.elem_p, ep)
+        assert m.np == npn
+
+
+def test_stress_uniaxial_closed_form(oracle):
+    c1, c2 = 2.0, 6.0
+    for lam in (1.0, 1.05, 1.2, 0.9):
+        F = np.diag([lam, lam ** -0.5, lam ** -0.5])
+        S, _ = oracle.point_stress(M.MR, [c1, c2], F, 0.0)
+        # sigma_xx - sigma_yy = 2 (lam^2 - 1/lam)(c1 + c2/lam), independent of p
+        assert abs((S[0] - S[1]) - 2.0 * (lam ** 2 - 1.0 / lam) * (c1 + c2 / lam)) < 1e-12 * (1 + abs(S[0]))
+        assert abs(S[1] - S[2]) < 1e-13 and np.all(np.abs(S[3:]) < 1e-13)
+        assert abs(S[0] + S[1] + S[2]) < 1e-12 * (1 + abs(S[0]))  # p = 0: deviatoric
+
+
+@pytest.mark.parametrize("nxi,pmode", [(2, "element"), (3, "node")])
+def test_patch_uniaxial_residual(oracle, nxi, pmode):
+    """Homogeneous uniaxial stretch: interior and pressure rows vanish, the
+    x = 1 face carries sigma_xx times the deformed face area."""
+    c1, c2, lam = 2.0, 6.0, 1.1
+    m = M.regular_box(2, 2, 2, nxi_u=nxi, pressure=pmode, materials=(c1, c2))
+    F = np.diag([lam, lam ** -0.5, lam ** -0.5])
+    S0, _ = oracle.point_stress(M.MR, [c1, c2], F, 0.0)
+    p_star = -S0[1]  # lateral traction free
+    x = np.concatenate([(F @ m.X).ravel(), np.full(m.n_pressure, p_star)])
+    P = oracle.Problem(m)
+    rp, col = P.pattern()
+    _, r = P.assemble(x, rp, col, jacobian=False)
+    nu = m.nu
+    i, j, k = m.node_ijk()
+    n1, n2, n3 = m.grid_u
+    sxx = 2.0 * (lam ** 2 - 1.0 / lam) * (c1 + c2 / lam)
+    scale = abs(sxx)
+    inner = (i > 0) & (i < n1 - 1) & (j > 0) & (j < n2 - 1) & (k > 0) & (k < n3 - 1)
+    for c in range(3):
+        assert np.all(np.abs(r[c * nu:(c + 1) * nu][inner]) < 1e-12 * scale)
+    assert np.all(np.abs(r[3 * nu:]) < 1e-13)
+    face = i == n1 - 1
+    assert abs(r[:nu][face].sum() - sxx / lam) < 1e-12 * scale
+    assert abs(r[:nu][i == 0].sum() + sxx / lam) < 1e-12 * scale
+    for c in (1, 2):
+        for sel in (face, i == 0):
+            assert abs(r[c * nu:(c + 1) * nu][sel].sum()) < 1e-12 * scale
+
+
+@pytest.mark.parametrize("name,mesh", small_meshes())
+def test_element_jacobian_matches_fd(oracle, name, mesh):
+    """Analytic element Jacobian vs the reference's one-sided FD rule."""
+    x = M.deformed_state(mesh, stretch=1.08, shear=0.04, noise=0.05, pressure=-1.5, seed=11)
+    P = oracle.Problem(mesh)
+    for e in (0, mesh.ne - 1):
+        K = P.element_jacobian(e, x)
+        Kfd = P.element_jacobian_fd(e, x)
+        assert np.array_equal(K, K.T)
+        err = np.abs(K - Kfd).max() / np.abs(K).max()
+        assert err < 1e-4, (name, e, err)  # one-sided rule: O(delta) truncation error
+        # central differences converge as O(h^2): the analytic tangent is the
+        # exact derivative of the residual, not just close to the FD rule
+        dofs = P.element_dofs(e)
+        h = 1e-5
+        Kc = np.zeros_like(K)
+        for j, d in enumerate(dofs):
+            xp, xm = x.copy(), x.copy()
+            xp[d] += h
+            xm[d] -= h
+            Kc[:, j] = (P.element_residual(e, xp) - P.element_residual(e, xm)) / (2 * h)
+        assert np.abs(K - Kc).max() / np.abs(K).max() < 1e-7, name
+
+
+def test_pattern_closed_form_counts(oracle):
+    # 9(3e+1)^3 + 2*3*(2e)^3 + e^3 for trilinear u / element-based p
+    for e in (1, 2, 4):
+        m = M.regular_box(e, e, e, nxi_u=2, pressure="element")
+        rp, col = oracle.Problem(m).pattern()
+        assert rp[-1] - 1 == 9 * (3 * e + 1) ** 3 + 2 * 3 * (2 * e) ** 3 + e ** 3
+    # 9(8e+1)^3 + 2*3*(5e+1)^3 + (3e+1)^3 for triquadratic u / trilinear p
+    for e in (1, 2, 3):
+        m = M.regular_box(e, e, e, nxi_u=3, pressure="node")
+        rp, col = oracle.Problem(m).pattern()
+        assert rp[-1] - 1 == 9 * (8 * e + 1) ** 3 + 2 * 3 * (5 * e + 1) ** 3 + (3 * e + 1) ** 3
+    m = M.regular_box(4, 4, 4, nxi_u=2, pressure="element")
+    assert oracle.Problem(m).pattern()[0][-1] - 1 == 22909
+
+
+def _desc(m, keep):
+    from cm_gb300 import _lib
+
+    def arr(a, dt):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dt)
+        keep.append(a)
+        return a.ctypes.data
+    d = _lib.FEMeshDesc()
+    mats = np.asarray(m.materials, dtype=np.float64)
+    d.num_elements, d.num_nodes_u, d.num_nodes_p = m.ne, m.nu, m.np
+    d.nodes_per_xi_u, d.pressure_interpolation, d.law = m.nxi_u, m.p_mode, m.law
+    d.num_material_components = mats.shape[-1]
+    d.materials_per_element = 1 if mats.ndim == 2 else 0
+    d.element_nodes_u = arr(m.elem_u, np.int32)
+    d.element_nodes_p = arr(m.elem_p, np.int32)
+    d.geometry = arr(m.X, np.float64)
+    d.materials = arr(mats, np.float64)
+    d.fibre_angles = arr(m.fibre, np.float64)
+    return d
+
+
+def product_pattern(m, base=1):
+    from cm_gb300 import _lib
+    L = _lib.load()
+    keep = []
+    d = _desc(m, keep)
+    nd, nnz = C.c_int64(), C.c_int64()
+    _lib.check(L.fe_structure_calculate(C.byref(d), base, C.byref(nd), C.byref(nnz), None, None))
+    rp = np.zeros(nd.value + 1, dtype=np.int32)
+    col = np.zeros(nnz.value, dtype=np.int32)
+    _lib.check(L.fe_structure_calculate(C.byref(d), base, C.byref(nd), C.byref(nnz), rp.ctypes.data,
+                                        col.ctypes.data))
+    return rp, col
+
+
+@pytest.mark.parametrize("name,mesh", small_meshes() + [
+    ("lin_elem_4", M.regular_box(4, 4, 4, nxi_u=2, pressure="element")),
+    ("quad_node_3x2x4", M.regular_box(3, 2, 4, nxi_u=3, pressure="node", perturb=0.1)),
+    ("lin_node", M.regular_box(3, 3, 2, nxi_u=2, pressure="node")),
+    ("quad_elem", M.regular_box(2, 3, 2, nxi_u=3, pressure="element")),
+])
+def test_product_pattern_bit_exact(oracle, name, mesh):
+    rp_o, col_o = oracle.Problem(mesh).pattern()
+    rp_p, col_p = product_pattern(mesh, base=1)
+    assert np.array_equal(rp_o, rp_p), name
+    assert np.array_equal(col_o, col_p), name
+    rp0, col0 = product_pattern(mesh, base=0)
+    assert np.array_equal(rp0 + 1, rp_p) and np.array_equal(col0 + 1, col_p)
+
+
+def test_product_rejects_bad_mesh():
+    from cm_gb300 import _lib
+    L = _lib.load()
+    m = M.regular_box(2, 2, 2, nxi_u=2)
+    keep = []
+    d = _desc(m, keep)
+    d.nodes_per_xi_u = 4
+    nd, nnz = C.c_int64(), C.c_int64()
+    assert L.fe_structure_calculate(C.byref(d), 1, C.byref(nd), C.byref(nnz), None, None) == _lib.FE_ERR_INVALID_ARGUMENT
+    assert "nodes_per_xi_u" in _lib.last_error()
+    d = _desc(m, keep)
+    bad = np.array(m.elem_u, dtype=np.int32)
+    bad[0, 0] = m.nu + 5
+    keep.append(bad)
+    d.element_nodes_u = bad.ctypes.data
+    assert L.fe_structure_calculate(C.byref(d), 1, C.byref(nd), C.byref(nnz), None, None) == _lib.FE_ERR_INVALID_ARGUMENT
+    d = _desc(m, keep)
+    d.law = 7
+    assert L.fe_structure_calculate(C.byref(d), 1, C.byref(nd), C.byref(nnz), None, None) == _lib.FE_ERR_INVALID_ARGUMENT
+
+
+def test_threaded_assembly_matches_serial(oracle):
+    m = M.regular_box(3, 3, 3, nxi_u=3, pressure="node", perturb=0.1, seed=2)
+    x = M.deformed_state(m, noise=0.05)
+    P = oracle.Problem(m)
+    rp, col = P.pattern()
+    v1, r1 = P.assemble(x, rp, col, nthreads=1)
+    v4, r4 = P.assemble(x, rp, col, nthreads=4)
+    assert np.allclose(v1, v4, rtol=1e-13, atol=1e-13 * np.abs(v1).max())
+    assert np.allclose(r1, r4, rtol=1e-13, atol=1e-13 * np.abs(r1).max())
+
+
+def test_assembled_jacobian_is_symmetric(oracle):
+    m = M.regular_box(2, 2, 2, nxi_u=3, pressure="node", perturb=0.1)
+    x = M.deformed_state(m, noise=0.05)
+    P = oracle.Problem(m)
+    rp, col = P.pattern()
+    v, _ = P.assemble(x, rp, col, residual=False)
+    import scipy.sparse as sp
+    A = sp.csr_matrix((v, col - 1, rp - 1), shape=(P.ndofs, P.ndofs))
+    assert abs(A - A.T).max() == 0.0
+
+
+def test_abi_exports_every_declared_symbol():
+    """libcm_fe.so loads and exports every function include/cm_fe.h declares."""
+    from cm_gb300 import _lib
+    header = open(os.path.join(ROOT, "include", "cm_fe.h")).read()
+    names = sorted(set(re.findall(r"^int (fe_\w+)\(", header, flags=re.M)))
+    assert len(names) >= 14
+    L = _lib.load()
+    for n in names:
+        assert hasattr(L, n), n
+        assert n in _lib.SIGNATURES, n
