@@ -46,6 +46,10 @@ def config_mesh(name):
                           perturb=0.1, seed=2)
         workload = ("32x32x32 triquadratic-u/trilinear-p box, MR c1=2 c2=6, interior nodes +-0.1h, "
                     "mixed-precision Jacobian + FP64 residual")
+    elif name == "cfg4":
+        m = M.regular_box(16, 16, 16, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0))
+        workload = ("16x16x16 triquadratic-u/trilinear-p unit cube, MR c1=2 c2=6, "
+                    "mixed-precision Jacobian + FP64 residual")
     elif name == "cfg1":
         m = M.regular_box(4, 4, 4, nxi_u=2, pressure="element", law=M.MR, materials=(2.0, 6.0))
         workload = "4x4x4 trilinear-u/element-p unit cube, MR c1=2 c2=6, FP64 Jacobian + residual"
@@ -205,7 +209,7 @@ def our_arm(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     m, x, workload = config_mesh(args.config)
-    mixed = args.config == "cfg2" and not args.fp64
+    mixed = args.config != "cfg1" and not args.fp64
     es = FiniteElasticityEquationsSet(m)
     dev = torch.device("cuda", local)
     xd = torch.from_numpy(x).to(dev)
@@ -347,7 +351,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="cfg2", choices=["cfg2", "cfg1"])
+    ap.add_argument("--config", default="cfg2", choices=["cfg2", "cfg4", "cfg1"])
     ap.add_argument("--fp64", action="store_true", help="time the FP64 path instead of the mixed path")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
