@@ -55,6 +55,38 @@ struct HostSetup {
   std::vector<double> gbf_u, gbf_p, gw;  // quadrature tables
 };
 
+// Arguments of the element kernels (plain data; device pointers).
+struct KParams {
+  int nu, law, nmat, matpe;
+  const int32_t* elem_u;
+  const int32_t* elem_p;
+  const double* geo;
+  const double* mat;
+  const double* gbf_u;
+  const double* gbf_p;
+  const double* gw;
+  const int32_t* row_ptr;
+  const int32_t* uu_row_ptr;
+  const int32_t* cp_row_ptr;
+  const int32_t* wu;
+  const int32_t* wp;
+  const uint16_t* tables;
+  const int32_t* elem_table;
+  const int32_t* elems;  // element list of this launch (NULL: first_elem + i)
+  int count;
+  int first_elem;
+  const double* x;
+  double* r;
+  double* vals;      // FP64 CSR values, or FP64 coupling values (mixed)
+  float* vals_uu;    // FP32 uu values (mixed)
+  double* elem_out;  // element-level output
+  unsigned* status;
+};
+
+// Launches the mixed-precision assembly kernel for one colour (fe_mixed.cu).
+// Returns a cudaError_t value.
+int launch_mixed(const HostSetup& s, const KParams& kp, int num_sms, void* stream);
+
 // Builds the set-up; returns FE_NO_ERROR or a FE_ERR_* code with msg filled.
 int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg);
 

@@ -32,8 +32,10 @@
 #include <type_traits>
 
 #include "fe_internal.h"
+#include "fe_math.cuh"
 
 using cmfe::HostSetup;
+using cmfe::KParams;
 using cmfe::NG;
 
 namespace {
@@ -52,40 +54,9 @@ int set_error(int code, const std::string& msg) {
       return set_error(FE_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(err__));      \
   } while (0)
 
-// ------------------------------------------------------------ constants ----
-__constant__ int c_T2V[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};   // TENSOR_TO_VOIGT3
-__constant__ int c_V2T[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};  // VOIGT_TO_TENSOR3
-
-constexpr double ZERO_TOL = 5.0 * 2.220446049250313e-16;  // ZERO_TOLERANCE (constants.f90:68)
-
 enum Mode { M_RES = 0, M_JAC = 1, M_MIX = 2, M_ERES = 3, M_EJAC = 4 };
 
-struct KParams {
-  int nu, law, nmat, matpe;
-  const int32_t* elem_u;
-  const int32_t* elem_p;
-  const double* geo;
-  const double* mat;
-  const double* gbf_u;
-  const double* gbf_p;
-  const double* gw;
-  const int32_t* row_ptr;
-  const int32_t* uu_row_ptr;
-  const int32_t* cp_row_ptr;
-  const int32_t* wu;
-  const int32_t* wp;
-  const uint16_t* tables;
-  const int32_t* elem_table;
-  const int32_t* elems;  // element list of this launch (NULL: first_elem + i)
-  int count;
-  int first_elem;
-  const double* x;
-  double* r;
-  double* vals;      // FP64 CSR values, or FP64 coupling values (mixed)
-  float* vals_uu;    // FP32 uu values (mixed)
-  double* elem_out;  // element-level output
-  unsigned* status;
-};
+
 
 template <int N1, int PM>
 struct Cfg {
@@ -114,232 +85,6 @@ struct Cfg {
   static constexpr int O_END = O_T + 6 * NPE * 3;
   static constexpr size_t SMEM = O_END * sizeof(double) + (NR + 4) * sizeof(int);
 };
-
-// ------------------------------------------------------- device maths ----
-__device__ __forceinline__ void d_inv3(const double a[3][3], double b[3][3], double& det) {
-  det = a[0][0] * a[1][1] * a[2][2] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
-        a[0][0] * a[2][1] * a[1][2] - a[1][0] * a[0][1] * a[2][2] - a[2][0] * a[1][1] * a[0][2];
-  if (fabs(det) > ZERO_TOL) {
-    b[0][0] = (a[1][1] * a[2][2] - a[2][1] * a[1][2]) / det;
-    b[1][0] = (a[1][2] * a[2][0] - a[2][2] * a[1][0]) / det;
-    b[2][0] = (a[1][0] * a[2][1] - a[2][0] * a[1][1]) / det;
-    b[0][1] = (a[2][1] * a[0][2] - a[0][1] * a[2][2]) / det;
-    b[1][1] = (a[2][2] * a[0][0] - a[0][2] * a[2][0]) / det;
-    b[2][1] = (a[2][0] * a[0][1] - a[0][0] * a[2][1]) / det;
-    b[0][2] = (a[0][1] * a[1][2] - a[1][1] * a[0][2]) / det;
-    b[1][2] = (a[0][2] * a[1][0] - a[1][2] * a[0][0]) / det;
-    b[2][2] = (a[0][0] * a[1][1] - a[1][0] * a[0][1]) / det;
-  } else {
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) b[i][j] = 0.0;
-  }
-}
-
-template <class T>
-__device__ __forceinline__ T d_pow_m13(T j);
-template <>
-__device__ __forceinline__ double d_pow_m13<double>(double j) { return pow(j, -1.0 / 3.0); }
-template <>
-__device__ __forceinline__ float d_pow_m13<float>(float j) { return powf(j, -1.0f / 3.0f); }
-template <class T>
-__device__ __forceinline__ T d_exp(T v);
-template <>
-__device__ __forceinline__ double d_exp<double>(double v) { return exp(v); }
-template <>
-__device__ __forceinline__ float d_exp<float>(float v) { return expf(v); }
-
-// Push-forward matrix t(F) of FINITE_ELASTICITY_PUSH_*_TENSOR (:1182-1253).
-template <class T>
-__device__ __forceinline__ void d_push_t(const T F[3][3], T t[6][6]) {
-#pragma unroll
-  for (int j = 0; j < 3; ++j)
-#pragma unroll
-    for (int i = 0; i < 6; ++i) t[i][j] = F[c_V2T[i][0]][c_V2T[j][0]] * F[c_V2T[i][1]][c_V2T[j][1]];
-#pragma unroll
-  for (int j = 3; j < 6; ++j)
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-      t[i][j] = F[c_V2T[i][0]][c_V2T[j][0]] * F[c_V2T[i][1]][c_V2T[j][1]] +
-                F[c_V2T[i][0]][c_V2T[j][1]] * F[c_V2T[i][1]][c_V2T[j][0]];
-}
-
-// F_bar = F J^(-1/3), AZL = F_bar^T F_bar, and the fictitious 2nd Piola
-// stress (and material tangent when C != nullptr) of MR (:4386-4394,
-// :684-699) or Guccione (:4419-4424, :758-781).
-template <class T>
-__device__ void d_fictitious(int law, const T* c, const T F[3][3], T J, T mod[3][3], T S[6], T (*C)[6]) {
-  const T s = d_pow_m13<T>(J);
-  T azl[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) mod[i][j] = F[i][j] * s;
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) azl[i][j] = mod[0][i] * mod[0][j] + mod[1][i] * mod[1][j] + mod[2][i] * mod[2][j];
-  if (law == FE_LAW_MOONEY_RIVLIN) {
-    const T I1 = azl[0][0] + azl[1][1] + azl[2][2];
-    const T t1 = T(-2.0) * c[1];
-    const T t2 = T(2.0) * (c[0] + I1 * c[1]);
-    S[0] = t1 * azl[0][0] + t2;
-    S[1] = t1 * azl[1][1] + t2;
-    S[2] = t1 * azl[2][2] + t2;
-    S[3] = t1 * azl[1][0];
-    S[4] = t1 * azl[2][0];
-    S[5] = t1 * azl[2][1];
-    if (C) {
-#pragma unroll
-      for (int i = 0; i < 6; ++i)
-#pragma unroll
-        for (int j = 0; j < 6; ++j) C[i][j] = T(0);
-      const T a = T(4.0) * c[1], b = T(-2.0) * c[1];
-      C[1][0] = a; C[2][0] = a; C[0][1] = a; C[2][1] = a; C[0][2] = a; C[1][2] = a;
-      C[3][3] = b; C[4][4] = b; C[5][5] = b;
-    }
-  } else {
-    const T B[6] = {T(2.0) * c[1], T(2.0) * c[2], T(2.0) * c[2], c[3], c[3], c[2]};
-    const T E[6] = {T(0.5) * (azl[0][0] - T(1.0)), T(0.5) * (azl[1][1] - T(1.0)), T(0.5) * (azl[2][2] - T(1.0)),
-                    azl[1][0], azl[2][0], azl[2][1]};
-    T DQ[6];
-    T dot = T(0);
-#pragma unroll
-    for (int i = 0; i < 6; ++i) DQ[i] = B[i] * E[i];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) dot = dot + E[i] * DQ[i];
-    const T t1 = T(0.5) * c[0] * d_exp<T>(T(0.5) * dot);
-#pragma unroll
-    for (int i = 0; i < 6; ++i) S[i] = t1 * DQ[i];
-    if (C) {
-#pragma unroll
-      for (int j = 0; j < 6; ++j)
-#pragma unroll
-        for (int i = j; i < 6; ++i) C[i][j] = t1 * DQ[i] * DQ[j];
-#pragma unroll
-      for (int i = 0; i < 6; ++i) C[i][i] = C[i][i] + t1 * B[i];
-#pragma unroll
-      for (int j = 1; j < 6; ++j)
-#pragma unroll
-        for (int i = 0; i < j; ++i) C[i][j] = C[j][i];
-    }
-  }
-}
-
-template <class T>
-__device__ __forceinline__ void d_push_stress(T S[6], const T t[6][6], T J) {
-  T r[6];
-#pragma unroll
-  for (int i = 0; i < 6; ++i) {
-    T s = T(0);
-#pragma unroll
-    for (int j = 0; j < 6; ++j) s = s + t[i][j] * S[j];
-    r[i] = s;
-  }
-#pragma unroll
-  for (int i = 0; i < 6; ++i) S[i] = r[i] / J;
-}
-
-// FINITE_ELASTICITY_GAUSS_STRESS_TENSOR (:4342-4454): Cauchy stress (Voigt).
-__device__ void d_gauss_stress(int law, const double* c, const double F[3][3], double J, double p, double S[6]) {
-  double mod[3][3], t[6][6];
-  d_fictitious<double>(law, c, F, J, mod, S, nullptr);
-  d_push_t<double>(mod, t);
-  d_push_stress<double>(S, t, J);
-  const double ot = (S[0] + S[1] + S[2]) / 3.0;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) S[i] = S[i] - ot + p;
-}
-
-// FINITE_ELASTICITY_GAUSS_ELASTICITY_TENSOR (:609-835): spatial tangent and
-// Cauchy stress (Voigt), in precision T.
-template <class T>
-__device__ void d_gauss_elasticity(int law, const T* c, const T F[3][3], T J, T p, T C[6][6], T S[6]) {
-  const T ONETHIRD = T(1.0) / T(3.0), TWOTHIRDS = T(2.0) / T(3.0);
-  const T DP[3][3] = {{TWOTHIRDS, -ONETHIRD, -ONETHIRD}, {-ONETHIRD, TWOTHIRDS, -ONETHIRD},
-                      {-ONETHIRD, -ONETHIRD, TWOTHIRDS}};
-  T mod[3][3], t[6][6];
-  d_fictitious<T>(law, c, F, J, mod, S, C);
-  d_push_t<T>(mod, t);
-  d_push_stress<T>(S, t, J);
-  {  // C <- t C t^T / J
-    T A[6][6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-#pragma unroll
-      for (int j = 0; j < 6; ++j) {
-        T s = T(0);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) s = s + t[i][k] * C[k][j];
-        A[i][j] = s;
-      }
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-#pragma unroll
-      for (int j = 0; j < 6; ++j) {
-        T s = T(0);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) s = s + A[i][k] * t[j][k];
-        C[i][j] = s / J;
-      }
-  }
-  const T trace = S[0] + S[1] + S[2];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) S[i] = S[i] - ONETHIRD * trace;
-  const T tt = TWOTHIRDS * trace;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) C[i][i] = C[i][i] + tt * (i < 3 ? T(1.0) : T(0.5));
-  T M[3][3], N[3][3], Q[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      T s = T(0);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) s = s + C[i][k] * DP[k][j];
-      M[i][j] = s;
-    }
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      T s = T(0);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) s = s + DP[i][k] * M[k][j];
-      N[i][j] = s;
-    }
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      T s = T(0);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) s = s + DP[i][k] * C[k][3 + j];
-      Q[i][j] = s;
-    }
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      C[i][j] = N[i][j];
-      C[i][3 + j] = Q[i][j];
-      C[3 + j][i] = Q[i][j];
-    }
-#pragma unroll
-  for (int j = 0; j < 6; ++j)
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-      const T ui = i < 3 ? TWOTHIRDS : T(0), uj = j < 3 ? TWOTHIRDS : T(0);
-      C[i][j] = C[i][j] - (ui * S[j] + uj * S[i]);
-    }
-#pragma unroll
-  for (int i = 0; i < 3; ++i) S[i] = S[i] + p;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) C[i][i] = C[i][i] - p;
-  C[1][0] = C[1][0] + p; C[2][0] = C[2][0] + p; C[0][1] = C[0][1] + p;
-  C[2][1] = C[2][1] + p; C[0][2] = C[0][2] + p; C[1][2] = C[1][2] + p;
-}
 
 // Block index of the (row comp m, col comp n) tempvec block: 0..2 diagonal,
 // 3,4,5 for (n,m) = (0,1), (0,2), (1,2).
@@ -526,8 +271,8 @@ __global__ void __launch_bounds__(128) fe_element_kernel(KParams P) {
           const double* rec = &s_gp[g * C::GPS];
           const double* dp = &s_dphi[(g * NPE + a) * 3];
           const double jgw = rec[9];
-          const double d = dp[0] * (jgw * rec[12 + c_T2V[0][m]]) + dp[1] * (jgw * rec[12 + c_T2V[1][m]]) +
-                           dp[2] * (jgw * rec[12 + c_T2V[2][m]]);
+          const double d = dp[0] * (jgw * rec[12 + t2v(0, m)]) + dp[1] * (jgw * rec[12 + t2v(1, m)]) +
+                           dp[2] * (jgw * rec[12 + t2v(2, m)]);
           acc = acc + d;
         }
       } else {
@@ -569,8 +314,8 @@ __global__ void __launch_bounds__(128) fe_element_kernel(KParams P) {
         for (int r = 0; r < 3; ++r)
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            const TT cv = (TT)rec[24 + c_T2V[r][mh] * 6 + c_T2V[c][nh]];
-            sub[r][c] = blk < 3 ? jgw * (cv + (TT)rec[18 + c_T2V[r][c]]) : jgw * cv;
+            const TT cv = (TT)rec[24 + t2v(r, mh) * 6 + t2v(c, nh)];
+            sub[r][c] = blk < 3 ? jgw * (cv + (TT)rec[18 + t2v(r, c)]) : jgw * cv;
           }
         const TT d0 = (TT)dpg[b * 3 + 0], d1 = (TT)dpg[b * 3 + 1], d2 = (TT)dpg[b * 3 + 2];
 #pragma unroll
@@ -1035,7 +780,13 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
   kp.vals_uu = du;
   kp.vals = dc;
   kp.r = dr;
-  if ((rc = run_colours<M_MIX>(h, kp, st))) return rc;
+  for (int c = 0; c < h->hs.ncolours; ++c) {
+    kp.elems = h->d_colour_elems + h->hs.colour_ptr[c];
+    kp.count = h->hs.colour_ptr[c + 1] - h->hs.colour_ptr[c];
+    const int e = cmfe::launch_mixed(h->hs, kp, h->num_sms, st);
+    if (e != 0) return set_error(FE_ERR_CUDA, std::string("mixed kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+    h->launches++;
+  }
   if (hu) CUDA_TRY(cudaMemcpyAsync(values_uu, du, sizeof(float) * h->hs.nnz_uu, cudaMemcpyDeviceToHost, st));
   if (hc) CUDA_TRY(cudaMemcpyAsync(values_coupling, dc, sizeof(double) * h->hs.nnz_cp, cudaMemcpyDeviceToHost, st));
   if (hr) CUDA_TRY(cudaMemcpyAsync(r, dr, sizeof(double) * h->hs.ndofs, cudaMemcpyDeviceToHost, st));

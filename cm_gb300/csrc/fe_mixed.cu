@@ -1,0 +1,575 @@
+// libcm_fe: mixed-precision element assembly (sm_103a).
+//
+// Same arithmetic content as the reference's element residual and Jacobian
+// (FiniteElasticity_FiniteElement{Residual,Jacobian}Evaluate,
+// finite_elasticity_routines.f90:1260-1639 and :842-1175), reorganised for
+// the GB300:
+//
+//  * FP64 only where the residual and the pressure coupling need it.  Per
+//    Gauss point the kinematics use the adjugate of dz/dxi (J_z dxi/dz =
+//    adj(dz/dxi), so no 3x3 division), the Cauchy stress is formed as
+//    F_bar S_bar F_bar^T / J (the push-forward of :1221-1253 written as a
+//    matrix product), and the residual is contracted against the fixed table
+//    of reference-element gradients: r(m,a) = sum_g sum_k dN_a/dxi_k (g) *
+//    P_g(k,m) with P_g = J_z w_g dxi/dz sigma.  The pressure-coupling block
+//    K(p_q, u_nb) = sum_g psi_q(g) J_z w_g dN_b/dz_n is contracted with the
+//    tensor-product (sum-factorised) form of the trilinear pressure basis.
+//  * The displacement block is FP32 with the contraction on tensor cores.
+//    Per Gauss point the spatial tangent is pulled back to xi space:
+//    D^{mn}(k,l) = sum_ij dxi_k/dz_i SUB^{mn}(i,j) dxi_l/dz_j with the
+//    reference's SUB^{mn} = J_z w (c(T2V(:,m),T2V(:,n)) + delta_mn sigma)
+//    (:1003-1034), so K^{mn}(a,b) = sum_{(g,k)} Phi(g,k;a) W^{mn}(g,k;b) with
+//    W = D Phi and Phi the constant gradient table.  That product runs as
+//    mma.sync m16n8k16 BF16 with FP32 accumulation; with SPLIT = 3 both
+//    operands are split into a BF16 high part and a BF16 residual and three
+//    products are accumulated, which keeps about 16 significant bits.
+//  * Elements of one colour share no node; a CTA processes EG elements at a
+//    time for the per-Gauss-point work (so 100+ threads do the FP64
+//    kinematics at once) and then contracts them one by one.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "fe_internal.h"
+#include "fe_math.cuh"
+
+using cmfe::HostSetup;
+using cmfe::KParams;
+using cmfe::NG;
+
+namespace {
+
+constexpr int align16(int x) { return (x + 15) & ~15; }
+
+template <int N1, int PM>
+struct MixCfg {
+  static constexpr int NPE = N1 * N1 * N1;
+  static constexpr int NPP = PM ? 8 : 1;
+  static constexpr int NR = NPE + NPP;
+  static constexpr int NU3 = 3 * NPE;
+  static constexpr int NROW = NU3 + NPP;
+  static constexpr int THREADS = 256;
+  static constexpr int EG = (N1 == 3) ? 4 : 8;  // elements per group
+  static constexpr int MT = (NPE + 15) / 16;    // m16 tiles over a
+  static constexpr int NT = (NPE + 7) / 8;      // n8 tiles over b
+  static constexpr int KT = 6;                  // k16 tiles over (g,k): 81 -> 96
+  static constexpr int KPW = 52;                // padded row length in 32-bit words (104 bf16)
+  static constexpr int AROWS = MT * 16;
+  static constexpr int BROWS = NT * 8;
+  static constexpr int REC64 = 20;  // P(9), A(9), t1, pad
+  static constexpr int REC32 = 56;  // D^{mn}(k,l) for 6 blocks, pad
+  static constexpr int O_PHI64 = 0;
+  static constexpr int O_PSI64 = align16(O_PHI64 + NG * 4 * NPE * 8);
+  static constexpr int O_L = align16(O_PSI64 + NG * 8 * 8);
+  static constexpr int O_W = align16(O_L + 6 * 8);
+  static constexpr int O_Z = align16(O_W + NG * 8);
+  static constexpr int O_P = align16(O_Z + EG * 3 * NPE * 8);
+  static constexpr int O_DZ = align16(O_P + EG * 8 * 8);
+  static constexpr int O_PG = align16(O_DZ + EG * NG * 9 * 8);
+  static constexpr int O_R64 = align16(O_PG + EG * NG * 8);
+  static constexpr int O_PHI32 = align16(O_R64 + EG * NG * REC64 * 8);
+  static constexpr int O_R32 = align16(O_PHI32 + NG * 3 * NPE * 4);
+  static constexpr int O_A = align16(O_R32 + EG * NG * REC32 * 4);
+  static constexpr int O_B = align16(O_A + 2 * AROWS * KPW * 4);
+  static constexpr int O_NODE = align16(O_B + 2 * BROWS * KPW * 4);
+  static constexpr int SMEM = align16(O_NODE + EG * (NR + 1) * 4);
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo_elem, hi_elem);  // .x -> low 16 bits
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// Splits (v0, v1) into BF16 high parts and BF16 residuals.
+__device__ __forceinline__ void split_bf16(float v0, float v1, uint32_t& hi, uint32_t& lo) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+  const float r0 = v0 - __bfloat162float(h.x);
+  const float r1 = v1 - __bfloat162float(h.y);
+  __nv_bfloat162 l = __floats2bfloat162_rn(r0, r1);
+  hi = *reinterpret_cast<uint32_t*>(&h);
+  lo = *reinterpret_cast<uint32_t*>(&l);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// Block (m, n) of the lower-triangle displacement blocks: 0..2 diagonal,
+// 3 = (1,0), 4 = (2,0), 5 = (2,1).
+__device__ __forceinline__ void blk_mn(int blk, int& m, int& n) {
+  m = blk < 3 ? blk : (blk == 3 ? 1 : 2);
+  n = blk < 3 ? blk : (blk == 5 ? 1 : 0);
+}
+
+// FP64 Cauchy stress of the MR or Guccione law from F (material frame) and
+// J = Jznu: sigma = dev(F_bar S_bar F_bar^T / J) + p I.
+__device__ void mix_stress(int law, const double* c, const double F[3][3], double J, double p, double sig[3][3]) {
+  const double s = rcbrt(J);
+  double Fb[3][3], Cb[3][3], S[3][3], T[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Fb[i][j] = F[i][j] * s;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i; j < 3; ++j) {
+      Cb[i][j] = Fb[0][i] * Fb[0][j] + Fb[1][i] * Fb[1][j] + Fb[2][i] * Fb[2][j];
+      Cb[j][i] = Cb[i][j];
+    }
+  if (law == FE_LAW_MOONEY_RIVLIN) {
+    const double I1 = Cb[0][0] + Cb[1][1] + Cb[2][2];
+    const double al = 2.0 * (c[0] + I1 * c[1]);
+    const double be = -2.0 * c[1];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) S[i][j] = be * Cb[i][j] + (i == j ? al : 0.0);
+  } else {
+    const double B[6] = {2.0 * c[1], 2.0 * c[2], 2.0 * c[2], c[3], c[3], c[2]};
+    const double E[6] = {0.5 * (Cb[0][0] - 1.0), 0.5 * (Cb[1][1] - 1.0), 0.5 * (Cb[2][2] - 1.0), Cb[1][0], Cb[2][0],
+                         Cb[2][1]};
+    double DQ[6], dot = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      DQ[i] = B[i] * E[i];
+      dot += E[i] * DQ[i];
+    }
+    const double t1 = 0.5 * c[0] * exp(0.5 * dot);
+    S[0][0] = t1 * DQ[0];
+    S[1][1] = t1 * DQ[1];
+    S[2][2] = t1 * DQ[2];
+    S[0][1] = S[1][0] = t1 * DQ[3];
+    S[0][2] = S[2][0] = t1 * DQ[4];
+    S[1][2] = S[2][1] = t1 * DQ[5];
+  }
+  // sigma_bar = F_bar S F_bar^T / J
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) T[i][j] = Fb[i][0] * S[0][j] + Fb[i][1] * S[1][j] + Fb[i][2] * S[2][j];
+  const double rJ = 1.0 / J;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i; j < 3; ++j) {
+      sig[i][j] = (T[i][0] * Fb[j][0] + T[i][1] * Fb[j][1] + T[i][2] * Fb[j][2]) * rJ;
+      sig[j][i] = sig[i][j];
+    }
+  const double tr3 = (sig[0][0] + sig[1][1] + sig[2][2]) * (1.0 / 3.0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) sig[i][i] = sig[i][i] - tr3 + p;
+}
+
+template <int N1, int PM, int SPLIT>
+__global__ void __launch_bounds__(256, 2) fe_mixed_kernel(KParams P) {
+  using C = MixCfg<N1, PM>;
+  constexpr int NPE = C::NPE, NPP = C::NPP, NR = C::NR, NU3 = C::NU3, NROW = C::NROW, EG = C::EG;
+  constexpr int KPW = C::KPW;
+  extern __shared__ __align__(16) unsigned char sm[];
+  double* s_phi = reinterpret_cast<double*>(sm + C::O_PHI64);  // [g][d][a]
+  double* s_psi = reinterpret_cast<double*>(sm + C::O_PSI64);  // [g][q]
+  double* s_L = reinterpret_cast<double*>(sm + C::O_L);        // [q][gi]
+  double* s_w = reinterpret_cast<double*>(sm + C::O_W);        // [g]
+  double* s_z = reinterpret_cast<double*>(sm + C::O_Z);        // [el][c][a]
+  double* s_p = reinterpret_cast<double*>(sm + C::O_P);        // [el][q]
+  double* s_dz = reinterpret_cast<double*>(sm + C::O_DZ);      // [el][g][c*3+k]
+  double* s_pg = reinterpret_cast<double*>(sm + C::O_PG);      // [el][g]
+  double* s_r64 = reinterpret_cast<double*>(sm + C::O_R64);    // [el][g][REC64]
+  float* s_phi32 = reinterpret_cast<float*>(sm + C::O_PHI32);  // [g][l][b]
+  float* s_r32 = reinterpret_cast<float*>(sm + C::O_R32);      // [el][g][REC32]
+  uint32_t* s_A = reinterpret_cast<uint32_t*>(sm + C::O_A);    // [hi/lo][a][KPW]
+  uint32_t* s_B = reinterpret_cast<uint32_t*>(sm + C::O_B);    // [hi/lo][b][KPW]
+  int* s_node = reinterpret_cast<int*>(sm + C::O_NODE);        // [el][NR+1]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nu = P.nu;
+
+  // ---- constant tables
+  for (int i = tid; i < NG * 4 * NPE; i += C::THREADS) s_phi[i] = P.gbf_u[i];
+  for (int i = tid; i < NG * 8; i += C::THREADS) s_psi[i] = P.gbf_p[i];
+  for (int i = tid; i < NG; i += C::THREADS) s_w[i] = P.gw[i];
+  if (tid < 6) {
+    const double x[3] = {(-sqrt(0.6) + 1.0) / 2.0, 0.5, (sqrt(0.6) + 1.0) / 2.0};
+    const int q = tid / 3, gi = tid % 3;
+    s_L[tid] = q == 0 ? 1.0 - x[gi] : x[gi];
+  }
+  for (int i = tid; i < NG * 3 * NPE; i += C::THREADS) {
+    const int g = i / (3 * NPE), l = (i / NPE) % 3, b = i % NPE;
+    s_phi32[i] = (float)P.gbf_u[(g * 4 + l + 1) * NPE + b];
+  }
+  for (int i = tid; i < C::AROWS * KPW; i += C::THREADS) {
+    const int a = i / KPW, wd = i % KPW;
+    float v[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int kap = 2 * wd + h;
+      v[h] = (a < NPE && kap < 3 * NG) ? (float)P.gbf_u[((kap / 3) * 4 + (kap % 3) + 1) * NPE + a] : 0.0f;
+    }
+    uint32_t hi, lo;
+    split_bf16(v[0], v[1], hi, lo);
+    s_A[i] = hi;
+    s_A[C::AROWS * KPW + i] = lo;
+  }
+
+  const int ngroups = (P.count + EG - 1) / EG;
+  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+    const int nvalid = min(EG, P.count - grp * EG);
+    __syncthreads();
+    // ---- P0: element nodes and table ids
+    for (int i = tid; i < EG * (NR + 1); i += C::THREADS) {
+      const int el = i / (NR + 1), r = i % (NR + 1);
+      int v = 0;
+      if (el < nvalid) {
+        const int e = P.elems[grp * EG + el];
+        if (r < NPE)
+          v = P.elem_u[(size_t)e * NPE + r];
+        else if (r < NR)
+          v = PM ? P.elem_p[(size_t)e * 8 + (r - NPE)] : e;
+        else
+          v = P.elem_table[e];
+      }
+      s_node[i] = v;
+    }
+    __syncthreads();
+    for (int i = tid; i < EG * 3 * NPE; i += C::THREADS) {
+      const int el = i / (3 * NPE), c = (i / NPE) % 3, a = i % NPE;
+      s_z[i] = el < nvalid ? P.x[(size_t)c * nu + s_node[el * (NR + 1) + a]] : 0.0;
+    }
+    for (int i = tid; i < EG * NPP; i += C::THREADS) {
+      const int el = i / NPP, q = i % NPP;
+      s_p[el * 8 + q] = el < nvalid ? P.x[(size_t)3 * nu + s_node[el * (NR + 1) + NPE + q]] : 0.0;
+    }
+    __syncthreads();
+    // ---- P1: dz/dxi and p at the Gauss points (FP64)
+    for (int i = tid; i < EG * NG * 9; i += C::THREADS) {
+      const int el = i / (NG * 9), g = (i / 9) % NG, c = (i / 3) % 3, k = i % 3;
+      const double* ph = &s_phi[(g * 4 + k + 1) * NPE];
+      const double* zc = &s_z[(el * 3 + c) * NPE];
+      double acc = 0.0;
+#pragma unroll
+      for (int a = 0; a < NPE; ++a) acc = fma(ph[a], zc[a], acc);
+      s_dz[i] = acc;
+    }
+    for (int i = tid; i < EG * NG; i += C::THREADS) {
+      const int el = i / NG, g = i % NG;
+      double pg;
+      if (PM) {
+        pg = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) pg = fma(s_psi[g * 8 + q], s_p[el * 8 + q], pg);
+      } else {
+        pg = s_p[el * 8];
+      }
+      s_pg[i] = pg;
+    }
+    __syncthreads();
+    // ---- P2: per Gauss point kinematics, FP64 stress, FP32 tangent in xi space
+    for (int t = tid; t < EG * NG; t += C::THREADS) {
+      const int el = t / NG, g = t % NG;
+      if (el >= nvalid) continue;
+      const int e = P.elems[grp * EG + el];
+      double M[3][3], adj[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) M[c][k] = s_dz[t * 9 + c * 3 + k];
+      adj[0][0] = M[1][1] * M[2][2] - M[1][2] * M[2][1];
+      adj[0][1] = M[0][2] * M[2][1] - M[0][1] * M[2][2];
+      adj[0][2] = M[0][1] * M[1][2] - M[0][2] * M[1][1];
+      adj[1][0] = M[1][2] * M[2][0] - M[1][0] * M[2][2];
+      adj[1][1] = M[0][0] * M[2][2] - M[0][2] * M[2][0];
+      adj[1][2] = M[0][2] * M[1][0] - M[0][0] * M[1][2];
+      adj[2][0] = M[1][0] * M[2][1] - M[1][1] * M[2][0];
+      adj[2][1] = M[0][1] * M[2][0] - M[0][0] * M[2][1];
+      adj[2][2] = M[0][0] * M[1][1] - M[0][1] * M[1][0];
+      const double det = M[0][0] * adj[0][0] + M[0][1] * adj[1][0] + M[0][2] * adj[2][0];
+      const double* geo = &P.geo[((size_t)e * NG + g) * 10];
+      double F[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) F[i][j] = M[i][0] * geo[j] + M[i][1] * geo[3 + j] + M[i][2] * geo[6 + j];
+      const double jx = geo[9];
+      const double jz = fabs(det);
+      const double jznu = jz / jx;
+      const double w = s_w[g];
+      const double sw = det > 0.0 ? w : -w;  // J_z w dxi/dz = sign(det) w adj
+      const double* cm = P.mat + (P.matpe ? (size_t)e * P.nmat : 0);
+      double cc[4] = {cm[0], cm[1], P.nmat > 2 ? cm[2] : 0.0, P.nmat > 3 ? cm[3] : 0.0};
+      const double pgv = s_pg[t];
+      double* rec = &s_r64[t * C::REC64];
+      bool ok = det > 0.0;
+      if (P.r != nullptr) {
+        double sig[3][3];
+        mix_stress(P.law, cc, F, jznu, pgv, sig);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            const double v = sw * (adj[k][0] * sig[0][m] + adj[k][1] * sig[1][m] + adj[k][2] * sig[2][m]);
+            rec[k * 3 + m] = v;
+            ok = ok && isfinite(v);
+          }
+        rec[18] = jx * w * (jznu - 1.0);
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int n = 0; n < 3; ++n) rec[9 + k * 3 + n] = sw * adj[k][n];
+      // FP32 tangent
+      float Ff[3][3], cf[4], Cf[6][6], Sf[6], inv[3][3];
+      const float rdet = 1.0f / (float)det;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          Ff[i][j] = (float)F[i][j];
+          inv[i][j] = (float)adj[i][j] * rdet;
+        }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) cf[i] = (float)cc[i];
+      d_gauss_elasticity<float>(P.law, cf, Ff, (float)jznu, (float)pgv, Cf, Sf);
+      const float jgwf = (float)(jz * w);
+      float* r32 = &s_r32[t * C::REC32];
+#pragma unroll
+      for (int blk = 0; blk < 6; ++blk) {
+        int m, n;
+        blk_mn(blk, m, n);
+        float sub[3][3], tmp[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            sub[i][j] = jgwf * (Cf[t2v(i, m)][t2v(j, n)] + (m == n ? Sf[t2v(i, j)] : 0.0f));
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) tmp[k][j] = inv[k][0] * sub[0][j] + inv[k][1] * sub[1][j] + inv[k][2] * sub[2][j];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int l = 0; l < 3; ++l)
+            r32[blk * 9 + k * 3 + l] = tmp[k][0] * inv[l][0] + tmp[k][1] * inv[l][1] + tmp[k][2] * inv[l][2];
+      }
+      ok = ok && isfinite(Cf[0][0]) && isfinite(Cf[3][3]);
+      if (!ok) atomicOr(P.status, 1u);
+    }
+    __syncthreads();
+    // ---- P3: residual rows and pressure-coupling columns (FP64)
+    const int n_res = P.r != nullptr ? EG * NROW : 0;
+    for (int it = tid; it < n_res + EG * NU3; it += C::THREADS) {
+      if (it < n_res) {
+        const int el = it / NROW, row = it % NROW;
+        if (el >= nvalid) continue;
+        const double* rec = &s_r64[el * NG * C::REC64];
+        const int* nd = &s_node[el * (NR + 1)];
+        const uint16_t* tab = P.tables + (size_t)nd[NR] * NR * NR;
+        double acc = 0.0;
+        int ln;
+        size_t R;
+        if (row < NU3) {
+          const int m = row / NPE, a = row % NPE;
+          for (int g = 0; g < NG; ++g) {
+            const double* ph = &s_phi[g * 4 * NPE + a];
+            const double* rg = &rec[g * C::REC64];
+            acc = fma(ph[NPE], rg[m], acc);
+            acc = fma(ph[2 * NPE], rg[3 + m], acc);
+            acc = fma(ph[3 * NPE], rg[6 + m], acc);
+          }
+          ln = a;
+          R = (size_t)m * nu + nd[a];
+        } else {
+          const int q = row - NU3;
+          for (int g = 0; g < NG; ++g) acc = PM ? fma(s_psi[g * 8 + q], rec[g * C::REC64 + 18], acc)
+                                                : acc + rec[g * C::REC64 + 18];
+          ln = NPE + q;
+          R = (size_t)3 * nu + nd[ln];
+        }
+        const bool first = tab[ln * NR + ln] & 0x8000;
+        P.r[R] = first ? acc : P.r[R] + acc;
+      } else {
+        const int j = it - n_res;
+        const int el = j / NU3, col = j % NU3;
+        if (el >= nvalid) continue;
+        const int n = col / NPE, b = col % NPE;
+        const double* rec = &s_r64[el * NG * C::REC64];
+        const int* nd = &s_node[el * (NR + 1)];
+        const uint16_t* tab = P.tables + (size_t)nd[NR] * NR * NR;
+        // V(g) = J_z w dN_b/dz_n at Gauss point g, folded into the xi1 stage
+        // of the sum-factorised pressure-basis contraction as it is produced.
+        double Kq[NPP];
+        double s1[2][9];
+        double vsum = 0.0;
+#pragma unroll
+        for (int jj = 0; jj < 9; ++jj) {
+          double v3[3];
+#pragma unroll
+          for (int g1 = 0; g1 < 3; ++g1) {
+            const int g = g1 + 3 * jj;
+            const double* ph = &s_phi[g * 4 * NPE + b];
+            const double* rg = &rec[g * C::REC64 + 9];
+            v3[g1] = fma(rg[n], ph[NPE], fma(rg[3 + n], ph[2 * NPE], rg[6 + n] * ph[3 * NPE]));
+          }
+          if (PM) {
+#pragma unroll
+            for (int q1 = 0; q1 < 2; ++q1)
+              s1[q1][jj] = fma(s_L[q1 * 3], v3[0], fma(s_L[q1 * 3 + 1], v3[1], s_L[q1 * 3 + 2] * v3[2]));
+          } else {
+            vsum += v3[0] + v3[1] + v3[2];
+          }
+        }
+        if (PM) {
+          double s2[2][2][3];
+#pragma unroll
+          for (int q1 = 0; q1 < 2; ++q1)
+#pragma unroll
+            for (int q2 = 0; q2 < 2; ++q2)
+#pragma unroll
+              for (int g3 = 0; g3 < 3; ++g3)
+                s2[q1][q2][g3] = fma(s_L[q2 * 3], s1[q1][3 * g3],
+                                     fma(s_L[q2 * 3 + 1], s1[q1][3 * g3 + 1], s_L[q2 * 3 + 2] * s1[q1][3 * g3 + 2]));
+#pragma unroll
+          for (int q = 0; q < NPP; ++q) {
+            const int q1 = q & 1, q2 = (q >> 1) & 1, q3 = q >> 2;
+            Kq[q] = fma(s_L[q3 * 3], s2[q1][q2][0], fma(s_L[q3 * 3 + 1], s2[q1][q2][1], s_L[q3 * 3 + 2] * s2[q1][q2][2]));
+          }
+        } else {
+          Kq[0] = vsum;
+        }
+        const int nb = nd[b];
+#pragma unroll
+        for (int q = 0; q < NPP; ++q) {
+          const int lq = NPE + q, pq = nd[lq];
+          const uint16_t tqb = tab[lq * NR + b], tbq = tab[b * NR + lq];
+          const size_t p1 = (size_t)P.cp_row_ptr[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (tqb & 0x7fff);
+          P.vals[p1] = (tqb & 0x8000) ? Kq[q] : P.vals[p1] + Kq[q];
+          const size_t p2 = (size_t)P.cp_row_ptr[(size_t)n * nu + nb] + (tbq & 0x7fff);
+          P.vals[p2] = (tbq & 0x8000) ? Kq[q] : P.vals[p2] + Kq[q];
+        }
+      }
+    }
+    // structurally zero pressure-pressure entries, stored by their first contributor
+    for (int i = tid; i < EG * NPP * NPP; i += C::THREADS) {
+      const int el = i / (NPP * NPP), q = (i / NPP) % NPP, q2 = i % NPP;
+      if (el >= nvalid) continue;
+      const int* nd = &s_node[el * (NR + 1)];
+      const uint16_t t = P.tables[(size_t)nd[NR] * NR * NR + (NPE + q) * NR + NPE + q2];
+      if (t & 0x8000) {
+        const int pq = nd[NPE + q];
+        P.vals[(size_t)P.cp_row_ptr[(size_t)3 * nu + pq] + 3 * (size_t)P.wp[pq] + (t & 0x7fff)] = 0.0;
+      }
+    }
+    // ---- P4: displacement blocks on tensor cores (FP32 accumulate)
+    for (int el = 0; el < nvalid; ++el) {
+      const int* nd = &s_node[el * (NR + 1)];
+      const uint16_t* tab = P.tables + (size_t)nd[NR] * NR * NR;
+      const float* r32 = &s_r32[el * NG * C::REC32];
+      for (int blk = 0; blk < 6; ++blk) {
+        __syncthreads();  // s_B free
+        for (int i = tid; i < C::BROWS * KPW; i += C::THREADS) {
+          const int b = i / KPW, wd = i % KPW;
+          float v[2];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int kap = 2 * wd + h;
+            float acc = 0.0f;
+            if (b < NPE && kap < 3 * NG) {
+              const int g = kap / 3, k = kap % 3;
+              const float* dt = &r32[g * C::REC32 + blk * 9 + k * 3];
+              const float* ph = &s_phi32[g * 3 * NPE + b];
+              acc = dt[0] * ph[0] + dt[1] * ph[NPE] + dt[2] * ph[2 * NPE];
+            }
+            v[h] = acc;
+          }
+          uint32_t hi, lo;
+          split_bf16(v[0], v[1], hi, lo);
+          s_B[i] = hi;
+          s_B[C::BROWS * KPW + i] = lo;
+        }
+        __syncthreads();
+        if (warp < C::MT * C::NT) {
+          const int mt = warp / C::NT, nt = warp % C::NT;
+          const int gq = lane >> 2, tq = lane & 3;
+          float d[4] = {0.f, 0.f, 0.f, 0.f};
+          const uint32_t* Ahi = s_A;
+          const uint32_t* Alo = s_A + C::AROWS * KPW;
+          const uint32_t* Bhi = s_B;
+          const uint32_t* Blo = s_B + C::BROWS * KPW;
+          const int r0 = (16 * mt + gq) * KPW, r1 = r0 + 8 * KPW, rb = (8 * nt + gq) * KPW;
+#pragma unroll
+          for (int kt = 0; kt < C::KT; ++kt) {
+            const int c0 = 8 * kt + tq, c1 = c0 + 4;
+            mma_bf16(d, Ahi[r0 + c0], Ahi[r1 + c0], Ahi[r0 + c1], Ahi[r1 + c1], Bhi[rb + c0], Bhi[rb + c1]);
+            if (SPLIT == 3) {
+              mma_bf16(d, Ahi[r0 + c0], Ahi[r1 + c0], Ahi[r0 + c1], Ahi[r1 + c1], Blo[rb + c0], Blo[rb + c1]);
+              mma_bf16(d, Alo[r0 + c0], Alo[r1 + c0], Alo[r0 + c1], Alo[r1 + c1], Bhi[rb + c0], Bhi[rb + c1]);
+            }
+          }
+          int m, n;
+          blk_mn(blk, m, n);
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const int a = 16 * mt + gq + (h >= 2 ? 8 : 0);
+            const int b = 8 * nt + 2 * tq + (h & 1);
+            if (a >= NPE || b >= NPE) continue;
+            if (m == n && a < b) continue;
+            const float v = d[h];
+            const int na = nd[a], nb = nd[b];
+            const uint16_t tab_ab = tab[a * NR + b];
+            const size_t p1 = (size_t)P.uu_row_ptr[(size_t)m * nu + na] + (size_t)n * P.wu[na] + (tab_ab & 0x7fff);
+            P.vals_uu[p1] = (tab_ab & 0x8000) ? v : P.vals_uu[p1] + v;
+            if (!(m == n && a == b)) {
+              const uint16_t tab_ba = tab[b * NR + a];
+              const size_t p2 =
+                  (size_t)P.uu_row_ptr[(size_t)n * nu + nb] + (size_t)m * P.wu[nb] + (tab_ba & 0x7fff);
+              P.vals_uu[p2] = (tab_ba & 0x8000) ? v : P.vals_uu[p2] + v;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+template <int N1, int PM, int SPLIT>
+int launch_t(const KParams& kp, int num_sms, cudaStream_t st) {
+  using C = MixCfg<N1, PM>;
+  static bool attr = false;
+  auto kern = fe_mixed_kernel<N1, PM, SPLIT>;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+    if (e != cudaSuccess) return (int)e;
+    attr = true;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::THREADS, C::SMEM);
+  if (e != cudaSuccess) return (int)e;
+  per_sm = per_sm < 1 ? 1 : per_sm;
+  const int groups = (kp.count + C::EG - 1) / C::EG;
+  int grid = per_sm * num_sms;
+  grid = grid < groups ? grid : groups;
+  grid = grid < 1 ? 1 : grid;
+  kern<<<grid, C::THREADS, C::SMEM, st>>>(kp);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace
+
+namespace cmfe {
+
+int launch_mixed(const HostSetup& s, const KParams& kp, int num_sms, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (kp.count <= 0) return 0;
+  if (s.n1 == 2 && s.pmode == 0) return launch_t<2, 0, 3>(kp, num_sms, st);
+  if (s.n1 == 2 && s.pmode == 1) return launch_t<2, 1, 3>(kp, num_sms, st);
+  if (s.n1 == 3 && s.pmode == 0) return launch_t<3, 0, 3>(kp, num_sms, st);
+  return launch_t<3, 1, 3>(kp, num_sms, st);
+}
+
+}  // namespace cmfe

@@ -5,7 +5,8 @@ where S is the largest magnitude of the element matrix / vector (element
 level) or of the assembled array (global level).  The absolute floor covers
 entries that cancel to (near) zero, whose rounding noise is set by the size
 of the terms, not by the entry.  The CSR pattern must match bit for bit.
-The FP32 block of the mixed path is checked at 2e-5 relative to S.
+The FP32 block of the mixed path (tensor-core contraction) is checked at
+MIXED_UU_TOL relative to S.
 """
 import numpy as np
 import pytest
@@ -118,28 +119,39 @@ def test_deterministic(torch):
     assert torch.equal(ua, ub) and torch.equal(ca, cb)
 
 
-@pytest.mark.parametrize("name", ["quad_node_mr_perturbed", "cfg1_lin_elem_mr", "quad_node_guccione_fibres"])
-def test_mixed_precision(torch, name):
+MIXED_UU_TOL = 1e-4  # BF16x3 tensor-core products, FP32 accumulation, relative to the largest entry
+
+
+@pytest.mark.parametrize("name", list(meshes()))
+def test_mixed_precision(torch, oracle, name):
+    """FP64 parts of the mixed path (coupling blocks, residual) match the
+    oracle at the FP64 tolerance; the FP32 displacement block matches it to
+    MIXED_UU_TOL of the largest entry."""
     m = meshes()[name]
-    x = torch.from_numpy(state(m)).cuda()
+    x = state(m)
+    P = oracle.Problem(m)
+    rp_o, col_o = P.pattern()
+    vo, ro = P.assemble(x, rp_o, col_o, nthreads=1)
     es = FiniteElasticityEquationsSet(m)
-    r64 = torch.empty_like(x)
-    v64 = es.jacobian_evaluate(x, r=r64).cpu().numpy()
-    rm = torch.empty_like(x)
-    vu, vc = es.jacobian_evaluate_mixed(x, r=rm)
-    es.check_status(x)
+    xd = torch.from_numpy(x).cuda()
+    rm = torch.empty_like(xd)
+    vu, vc = es.jacobian_evaluate_mixed(xd, r=rm)
+    es.check_status(xd)
     full = es.mixed_to_full(vu.cpu().numpy(), vc.cpu().numpy())
     uu_rp, cp_rp = es.mixed_layout()
     rp, _ = es.csr_pattern()
     is_uu = np.zeros(es.nnz, dtype=bool)
     for r in range(3 * m.nu):
         is_uu[rp[r]:rp[r] + (uu_rp[r + 1] - uu_rp[r])] = True
-    # FP64 parts: identical arithmetic to the FP64 path
-    assert np.array_equal(full[~is_uu], v64[~is_uu])
-    assert torch.equal(rm, r64)
-    # FP32 tangent block
-    S = np.abs(v64).max()
-    assert np.abs(full[is_uu] - v64[is_uu]).max() < 2e-5 * S
+    assert_entrywise(full[~is_uu], vo[~is_uu], what=name + " mixed coupling blocks")
+    assert_entrywise(rm.cpu().numpy(), ro, what=name + " mixed residual")
+    S = np.abs(vo).max()
+    err = np.abs(full[is_uu] - vo[is_uu]).max() / S
+    assert err < MIXED_UU_TOL, (name, err)
+    # exact symmetry of the assembled FP32 block (mirrored like the reference)
+    import scipy.sparse as sp
+    A = sp.csr_matrix((full, col_o - 1, rp_o - 1), shape=(es.ndofs, es.ndofs))
+    assert abs(A - A.T).max() == 0.0
 
 
 def test_inverted_element_reports_numerical_error(torch):
@@ -209,7 +221,7 @@ def test_full_size_config2_properties(torch, oracle):
     uu_pos = np.concatenate([np.arange(uu_rp[i], uu_rp[i + 1]) for i in range(0, nu3, 997)])
     d64 = vals[torch.from_numpy(uu_idx).cuda()]
     d32 = vu[torch.from_numpy(uu_pos).cuda()].double()
-    assert float((d64 - d32).abs().max()) < 2e-5 * float(vals.abs().max())
+    assert float((d64 - d32).abs().max()) < MIXED_UU_TOL * float(vals.abs().max())
 
 
 def test_native_library_launches(torch):
