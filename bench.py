@@ -253,6 +253,25 @@ def our_arm(args):
     step_s = t / args.steps
     value = world * m.ne / step_s
 
+    # the same mixed assembly with double-float high-precision phases
+    dfloat = None
+    if mixed:
+        es.set_high_precision("double_float")
+        step()
+        torch.cuda.synchronize(dev)
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        for _ in range(args.steps):
+            step()
+        s1.record(stream)
+        s1.synchronize()
+        es.check_status(xd)
+        tdf = s0.elapsed_time(s1) / 1e3 / args.steps
+        dfloat = {"value": m.ne / tdf, "unit": UNIT, "ms_per_step": 1e3 * tdf,
+                  "dtype": "fp32+double-float (FP32 pairs, ~48-bit) residual/coupling",
+                  "roofline_frac_hbm": algorithmic_bytes(m, es, True) / tdf / 1e9 / peaks()["hbm_gbs"]}
+        es.set_high_precision("fp64")
+
     # FP64 path on the same workload (the plain comparator)
     plain = None
     if mixed:
@@ -329,6 +348,8 @@ def our_arm(args):
     }
     if plain:
         out["plain_fp64"] = plain
+    if dfloat:
+        out["mixed_double_float"] = dfloat
     if world == 1 and not args.no_cpu:
         rp1, col1 = es.csr_pattern(base=1)
         out["cpu_baseline"] = cpu_baseline(m, x, rp1, col1)

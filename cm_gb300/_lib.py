@@ -24,6 +24,8 @@ FE_ERR_PATTERN = -6
 
 FE_LAW_MOONEY_RIVLIN = 1
 FE_LAW_GUCCIONE = 15
+FE_HIGH_PRECISION_FP64 = 0
+FE_HIGH_PRECISION_DOUBLE_FLOAT = 1
 FE_PRESSURE_ELEMENT_BASED = 0
 FE_PRESSURE_NODE_BASED = 1
 
@@ -59,6 +61,7 @@ SIGNATURES = {
     "fe_element_size": [_vp, C.POINTER(_i32)],
     "fe_element_residuals": [_vp, _vp, _i32, _i32, _vp, _vp],
     "fe_element_jacobians": [_vp, _vp, _i32, _i32, _vp, _vp],
+    "fe_set_high_precision": [_vp, _i32],
     "fe_check": [_vp, _vp],
     "fe_launch_count": [_vp, C.POINTER(_i64)],
     "fe_last_error": [C.c_char_p, _i32],

@@ -61,6 +61,7 @@ struct KParams {
   const int32_t* elem_u;
   const int32_t* elem_p;
   const double* geo;
+  const float* geo_dd;  // geo as (hi, lo) FP32 pairs, for the double-float variant
   const double* mat;
   const double* gbf_u;
   const double* gbf_p;
@@ -80,12 +81,14 @@ struct KParams {
   double* vals;      // FP64 CSR values, or FP64 coupling values (mixed)
   float* vals_uu;    // FP32 uu values (mixed)
   double* elem_out;  // element-level output
+  int res_only;      // mixed kernel: residual only (no Jacobian blocks)
   unsigned* status;
 };
 
-// Launches the mixed-precision assembly kernel for one colour (fe_mixed.cu).
+// Launches the mixed-precision assembly kernel for one colour (fe_mixed.cu),
+// with the high-precision phases in FP64 or in double-float arithmetic.
 // Returns a cudaError_t value.
-int launch_mixed(const HostSetup& s, const KParams& kp, int num_sms, void* stream);
+int launch_mixed(const HostSetup& s, const KParams& kp, int num_sms, void* stream, bool double_float);
 
 // Builds the set-up; returns FE_NO_ERROR or a FE_ERR_* code with msg filled.
 int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg);

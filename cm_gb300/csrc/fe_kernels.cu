@@ -451,6 +451,8 @@ struct fe_equations_set {
           *d_colour_elems = nullptr;
   uint16_t* d_tables = nullptr;
   double *d_geo = nullptr, *d_mat = nullptr, *d_gbf_u = nullptr, *d_gbf_p = nullptr, *d_gw = nullptr;
+  float* d_geo_dd = nullptr;
+  int high_precision = FE_HIGH_PRECISION_FP64;
   unsigned* d_status = nullptr;
   // staging for calls given host memory
   double *s_x = nullptr, *s_r = nullptr, *s_vals = nullptr, *s_cp = nullptr, *s_elem = nullptr;
@@ -503,6 +505,7 @@ KParams base_params(fe_handle h) {
   k.elem_u = h->d_elem_u;
   k.elem_p = h->d_elem_p;
   k.geo = h->d_geo;
+  k.geo_dd = h->d_geo_dd;
   k.mat = h->d_mat;
   k.gbf_u = h->d_gbf_u;
   k.gbf_p = h->d_gbf_p;
@@ -621,6 +624,15 @@ int fe_create(const fe_mesh_desc* desc, fe_handle* out) {
       (rc = dev_upload(&h->d_gbf_u, s.gbf_u)) || (rc = dev_upload(&h->d_gbf_p, s.gbf_p)) ||
       (rc = dev_upload(&h->d_gw, s.gw)))
     return fail(rc);
+  {
+    std::vector<float> gdd(s.geo.size() * 2);
+    for (size_t i = 0; i < s.geo.size(); ++i) {
+      const float hi = (float)s.geo[i];
+      gdd[2 * i] = hi;
+      gdd[2 * i + 1] = (float)(s.geo[i] - (double)hi);
+    }
+    if ((rc = dev_upload(&h->d_geo_dd, gdd))) return fail(rc);
+  }
   if (cudaMalloc(&h->d_status, sizeof(unsigned)) != cudaSuccess ||
       cudaMemset(h->d_status, 0, sizeof(unsigned)) != cudaSuccess)
     return fail(set_error(FE_ERR_CUDA, "status allocation failed"));
@@ -630,7 +642,7 @@ int fe_create(const fe_mesh_desc* desc, fe_handle* out) {
 
 int fe_destroy(fe_handle h) {
   if (!h) return FE_NO_ERROR;
-  void* ptrs[] = {h->d_elem_u, h->d_elem_p, h->d_row_ptr, h->d_uu_row_ptr, h->d_cp_row_ptr, h->d_wu,
+  void* ptrs[] = {h->d_geo_dd, h->d_elem_u, h->d_elem_p, h->d_row_ptr, h->d_uu_row_ptr, h->d_cp_row_ptr, h->d_wu,
                   h->d_wp, h->d_elem_table, h->d_colour_elems, h->d_tables, h->d_geo, h->d_mat,
                   h->d_gbf_u, h->d_gbf_p, h->d_gw, h->d_status, h->s_x, h->s_r, h->s_vals, h->s_cp,
                   h->s_uu, h->s_elem};
@@ -708,7 +720,14 @@ int fe_residual_evaluate(fe_handle h, const double* x, double* r, void* stream) 
   KParams kp = base_params(h);
   kp.x = dx;
   kp.r = dr;
-  if ((rc = run_colours<M_RES>(h, kp, st))) return rc;
+  kp.res_only = 1;
+  for (int c = 0; c < h->hs.ncolours; ++c) {
+    kp.elems = h->d_colour_elems + h->hs.colour_ptr[c];
+    kp.count = h->hs.colour_ptr[c + 1] - h->hs.colour_ptr[c];
+    const int e = cmfe::launch_mixed(h->hs, kp, h->num_sms, st, h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT);
+    if (e != 0) return set_error(FE_ERR_CUDA, std::string("residual kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+    h->launches++;
+  }
   if (hr) {
     CUDA_TRY(cudaMemcpyAsync(r, dr, sizeof(double) * h->hs.ndofs, cudaMemcpyDeviceToHost, st));
     return finish_status(h, st);
@@ -783,7 +802,7 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
   for (int c = 0; c < h->hs.ncolours; ++c) {
     kp.elems = h->d_colour_elems + h->hs.colour_ptr[c];
     kp.count = h->hs.colour_ptr[c + 1] - h->hs.colour_ptr[c];
-    const int e = cmfe::launch_mixed(h->hs, kp, h->num_sms, st);
+    const int e = cmfe::launch_mixed(h->hs, kp, h->num_sms, st, h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT);
     if (e != 0) return set_error(FE_ERR_CUDA, std::string("mixed kernel launch: ") + cudaGetErrorString((cudaError_t)e));
     h->launches++;
   }
@@ -840,6 +859,14 @@ int fe_element_residuals(fe_handle h, const double* x, int32_t first, int32_t co
 
 int fe_element_jacobians(fe_handle h, const double* x, int32_t first, int32_t count, double* out, void* stream) {
   return element_eval(h, x, first, count, out, stream, true);
+}
+
+int fe_set_high_precision(fe_handle h, int32_t mode) {
+  if (!h) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL handle");
+  if (mode != FE_HIGH_PRECISION_FP64 && mode != FE_HIGH_PRECISION_DOUBLE_FLOAT)
+    return set_error(FE_ERR_INVALID_ARGUMENT, "unknown high-precision mode");
+  h->high_precision = mode;
+  return FE_NO_ERROR;
 }
 
 int fe_check(fe_handle h, void* stream) {

@@ -162,6 +162,14 @@ class FiniteElasticityEquationsSet:
         return out.reshape(count, n, n).transpose(1, 2) if not isinstance(out, np.ndarray) else \
             out.reshape(count, n, n).transpose(0, 2, 1)
 
+    def set_high_precision(self, mode: str):
+        """'fp64' (IEEE binary64, default) or 'double_float' (FP32 pairs, about
+        48 significant bits) for the residual and pressure-coupling parts of
+        residual_evaluate and jacobian_evaluate_mixed."""
+        code = {"fp64": _lib.FE_HIGH_PRECISION_FP64, "double_float": _lib.FE_HIGH_PRECISION_DOUBLE_FLOAT}[mode]
+        check(_lib.load().fe_set_high_precision(self._h, code))
+        self.high_precision = mode
+
     def check_status(self, x=None):
         check(_lib.load().fe_check(self._h, _stream(x)))
 

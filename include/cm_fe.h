@@ -136,6 +136,17 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
 int fe_mixed_layout(fe_handle h, int64_t* nnz_uu, int64_t* nnz_coupling, int32_t* uu_row_ptr,
                     int32_t* cp_row_ptr);
 
+/* Arithmetic of the high-precision parts of fe_residual_evaluate and
+ * fe_jacobian_evaluate_mixed (the residual and the displacement-pressure
+ * coupling blocks).  FE_HIGH_PRECISION_FP64 (the default) uses IEEE binary64.
+ * FE_HIGH_PRECISION_DOUBLE_FLOAT uses unevaluated pairs of FP32 numbers
+ * (about 48 significant bits) on the FP32 pipes, which GB300 runs far faster
+ * than its FP64 pipe; results stay within about 1e-13 relative of FP64.
+ * No counterpart in the reference (which runs FP64 only). */
+#define FE_HIGH_PRECISION_FP64 0
+#define FE_HIGH_PRECISION_DOUBLE_FLOAT 1
+int fe_set_high_precision(fe_handle h, int32_t mode);
+
 /* Element-level evaluation for a contiguous range of elements (0-based), the
  * direct counterparts of FiniteElasticity_FiniteElementResidualEvaluate /
  * ..JacobianEvaluate(EQUATIONS_SET, ELEMENT_NUMBER).  Element matrices are

@@ -120,19 +120,26 @@ def test_deterministic(torch):
 
 
 MIXED_UU_TOL = 1e-4  # BF16x3 tensor-core products, FP32 accumulation, relative to the largest entry
+# Double-float (FP32 pair, ~48-bit) high-precision phases: per-entry tolerance
+# 1e-11 relative with a 1e-12 S floor (FP64 mode uses the FP64 tolerance).
+REL_DD, FLOOR_DD = 1e-11, 1e-12
 
 
+@pytest.mark.parametrize("mode", ["fp64", "double_float"])
 @pytest.mark.parametrize("name", list(meshes()))
-def test_mixed_precision(torch, oracle, name):
-    """FP64 parts of the mixed path (coupling blocks, residual) match the
-    oracle at the FP64 tolerance; the FP32 displacement block matches it to
-    MIXED_UU_TOL of the largest entry."""
+def test_mixed_precision(torch, oracle, name, mode):
+    """High-precision parts of the mixed path (coupling blocks, residual)
+    match the oracle at the FP64 tolerance (fp64 mode) or the double-float
+    tolerance; the FP32 displacement block matches it to MIXED_UU_TOL of the
+    largest entry."""
     m = meshes()[name]
     x = state(m)
     P = oracle.Problem(m)
     rp_o, col_o = P.pattern()
     vo, ro = P.assemble(x, rp_o, col_o, nthreads=1)
     es = FiniteElasticityEquationsSet(m)
+    es.set_high_precision(mode)
+    rel, floor = (REL, FLOOR) if mode == "fp64" else (REL_DD, FLOOR_DD)
     xd = torch.from_numpy(x).cuda()
     rm = torch.empty_like(xd)
     vu, vc = es.jacobian_evaluate_mixed(xd, r=rm)
@@ -143,8 +150,10 @@ def test_mixed_precision(torch, oracle, name):
     is_uu = np.zeros(es.nnz, dtype=bool)
     for r in range(3 * m.nu):
         is_uu[rp[r]:rp[r] + (uu_rp[r + 1] - uu_rp[r])] = True
-    assert_entrywise(full[~is_uu], vo[~is_uu], what=name + " mixed coupling blocks")
-    assert_entrywise(rm.cpu().numpy(), ro, what=name + " mixed residual")
+    assert_entrywise(full[~is_uu], vo[~is_uu], rel, floor, what=name + " mixed coupling blocks")
+    assert_entrywise(rm.cpu().numpy(), ro, rel, floor, what=name + " mixed residual")
+    r_only = es.residual_evaluate(xd)
+    assert torch.equal(r_only, rm)
     S = np.abs(vo).max()
     err = np.abs(full[is_uu] - vo[is_uu]).max() / S
     assert err < MIXED_UU_TOL, (name, err)
