@@ -289,7 +289,10 @@ __global__ void __launch_bounds__(128) fe_element_kernel(KParams P) {
         const int ln = tid < NU3 ? tid % NPE : NPE + (tid - NU3);
         const size_t R = tid < NU3 ? (size_t)(tid / NPE) * P.nu + s_node[ln] : (size_t)3 * P.nu + s_node[ln];
         const bool first = tab[ln * NR + ln] & 0x8000;
-        P.r[R] = first ? acc : P.r[R] + acc;
+        if (first)
+          P.r[R] = acc;
+        else
+          atomicAdd(&P.r[R], acc);
       }
     }
     if (!JAC) continue;
@@ -382,17 +385,29 @@ __global__ void __launch_bounds__(128) fe_element_kernel(KParams P) {
         const TT v = acc_uu[j];
         if (MIX) {
           const size_t p1 = (size_t)P.uu_row_ptr[(size_t)m * nu + na] + (size_t)n * P.wu[na] + (tab_ab & 0x7fff);
-          P.vals_uu[p1] = (tab_ab & 0x8000) ? (float)v : P.vals_uu[p1] + (float)v;
+          if (tab_ab & 0x8000)
+            P.vals_uu[p1] = (float)v;
+          else
+            atomicAdd(&P.vals_uu[p1], (float)v);
           if (R != Cc) {
             const size_t p2 = (size_t)P.uu_row_ptr[(size_t)n * nu + nb] + (size_t)m * P.wu[nb] + (tab_ba & 0x7fff);
-            P.vals_uu[p2] = (tab_ba & 0x8000) ? (float)v : P.vals_uu[p2] + (float)v;
+            if (tab_ba & 0x8000)
+              P.vals_uu[p2] = (float)v;
+            else
+              atomicAdd(&P.vals_uu[p2], (float)v);
           }
         } else {
           const size_t p1 = (size_t)P.row_ptr[(size_t)m * nu + na] + (size_t)n * P.wu[na] + (tab_ab & 0x7fff);
-          P.vals[p1] = (tab_ab & 0x8000) ? (double)v : P.vals[p1] + (double)v;
+          if (tab_ab & 0x8000)
+            P.vals[p1] = (double)v;
+          else
+            atomicAdd(&P.vals[p1], (double)v);
           if (R != Cc) {
             const size_t p2 = (size_t)P.row_ptr[(size_t)n * nu + nb] + (size_t)m * P.wu[nb] + (tab_ba & 0x7fff);
-            P.vals[p2] = (tab_ba & 0x8000) ? (double)v : P.vals[p2] + (double)v;
+            if (tab_ba & 0x8000)
+              P.vals[p2] = (double)v;
+            else
+              atomicAdd(&P.vals[p2], (double)v);
           }
         }
       }
@@ -409,11 +424,17 @@ __global__ void __launch_bounds__(128) fe_element_kernel(KParams P) {
         const uint16_t t_qb = tab[lq * NR + b], t_bq = tab[b * NR + lq];
         const double v = acc_pu[j];
         const size_t p1 = (size_t)rp[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (t_qb & 0x7fff);
-        P.vals[p1] = (t_qb & 0x8000) ? v : P.vals[p1] + v;
+        if ((t_qb & 0x8000))
+          P.vals[p1] = v;
+        else
+          atomicAdd(&P.vals[p1], v);
         // mirror: displacement row (n, b), pressure column q
         const size_t p2 = MIX ? (size_t)rp[(size_t)n * nu + nb] + (t_bq & 0x7fff)
                               : (size_t)rp[(size_t)n * nu + nb] + 3 * (size_t)P.wu[nb] + (t_bq & 0x7fff);
-        P.vals[p2] = (t_bq & 0x8000) ? v : P.vals[p2] + v;
+        if ((t_bq & 0x8000))
+          P.vals[p2] = v;
+        else
+          atomicAdd(&P.vals[p2], v);
       }
     }
     // structurally zero pressure-pressure entries: stored by their first contributor

@@ -59,7 +59,9 @@ struct MixCfg {
   static constexpr int AROWS = MT * 16;
   static constexpr int BROWS = NT * 8;
   static constexpr int REC64 = 20;  // P(9), A(9), t1, pad
-  static constexpr int REC32 = 56;  // D^{mn}(k,l) for 6 blocks, pad
+  static constexpr int REC32 = 60;  // D^{mn}(k,l) for 6 blocks, padded so Gauss points 2 apart hit banks 24 apart
+  static constexpr int PHS = 84;    // per-Gauss-point stride of the FP32 gradient table (conflict-free fragment loads)
+  static constexpr int KAP = 84;    // contraction length: kappa = 28 k + g, g < 27 (g = 27 is padding)
   static constexpr int O_PHI64 = 0;
   static constexpr int O_PSI64 = align16(O_PHI64 + NG * 4 * NPE * 8);
   static constexpr int O_L = align16(O_PSI64 + NG * 8 * 8);
@@ -71,7 +73,7 @@ struct MixCfg {
   static constexpr int O_PG = align16(O_DZ + EG * NG * 9 * 8);
   static constexpr int O_R64 = align16(O_PG + EG * NG * 8);
   static constexpr int O_PHI32 = align16(O_R64 + EG * NG * REC64 * 8);
-  static constexpr int O_R32 = align16(O_PHI32 + NG * 3 * NPE * 4);
+  static constexpr int O_R32 = align16(O_PHI32 + NG * PHS * 4);
   static constexpr int O_A = align16(O_R32 + EG * NG * REC32 * 4);
   static constexpr int O_F32 = align16(O_A + 2 * AROWS * KPW * 4);
   static constexpr int O_NODE = align16(O_F32 + EG * NG * 24 * 4);
@@ -240,7 +242,7 @@ __global__ void __launch_bounds__(256, 2) fe_mixed_kernel(KParams P) {
   }
   for (int i = tid; i < NG * 3 * NPE; i += C::THREADS) {
     const int g = i / (3 * NPE), l = (i / NPE) % 3, b = i % NPE;
-    s_phi32[i] = (float)P.gbf_u[(g * 4 + l + 1) * NPE + b];
+    s_phi32[g * C::PHS + l * NPE + b] = (float)P.gbf_u[(g * 4 + l + 1) * NPE + b];
   }
   for (int i = tid; i < C::AROWS * KPW; i += C::THREADS) {
     const int a = i / KPW, wd = i % KPW;
@@ -248,7 +250,8 @@ __global__ void __launch_bounds__(256, 2) fe_mixed_kernel(KParams P) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int kap = 2 * wd + h;
-      v[h] = (a < NPE && kap < 3 * NG) ? (float)P.gbf_u[((kap / 3) * 4 + (kap % 3) + 1) * NPE + a] : 0.0f;
+      const int kk = kap / 28, gg = kap % 28;
+      v[h] = (a < NPE && kap < C::KAP && gg < NG) ? (float)P.gbf_u[(gg * 4 + kk + 1) * NPE + a] : 0.0f;
     }
     uint32_t hi, lo;
     split_bf16(v[0], v[1], hi, lo);
@@ -488,7 +491,10 @@ __global__ void __launch_bounds__(256, 2) fe_mixed_kernel(KParams P) {
         }
         const bool first = tab[ln * NR + ln] & 0x8000;
         const double accd = hd(acc);
-        P.r[R] = first ? accd : P.r[R] + accd;
+        if (first)
+          P.r[R] = accd;
+        else
+          atomicAdd(&P.r[R], accd);
       } else {
         const int j = it - n_res;
         const int el = j / NU3, col = j % NU3;
@@ -545,9 +551,15 @@ __global__ void __launch_bounds__(256, 2) fe_mixed_kernel(KParams P) {
           const uint16_t tqb = tab[lq * NR + b], tbq = tab[b * NR + lq];
           const double kv = hd(Kq[q]);
           const size_t p1 = (size_t)P.cp_row_ptr[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (tqb & 0x7fff);
-          P.vals[p1] = (tqb & 0x8000) ? kv : P.vals[p1] + kv;
+          if ((tqb & 0x8000))
+            P.vals[p1] = kv;
+          else
+            atomicAdd(&P.vals[p1], kv);
           const size_t p2 = (size_t)P.cp_row_ptr[(size_t)n * nu + nb] + (tbq & 0x7fff);
-          P.vals[p2] = (tbq & 0x8000) ? kv : P.vals[p2] + kv;
+          if ((tbq & 0x8000))
+            P.vals[p2] = kv;
+          else
+            atomicAdd(&P.vals[p2], kv);
         }
       }
     }
@@ -565,7 +577,7 @@ __global__ void __launch_bounds__(256, 2) fe_mixed_kernel(KParams P) {
     // ---- P4: displacement blocks on tensor cores (FP32 accumulate).
     // The six lower blocks of one element are stacked along M:
     //   D'[(blk,b)][a] = sum_kappa W^{blk}[kappa][b] Phi[kappa][a] = K^{blk}(a,b),
-    // kappa = 3g + k.  Each warp owns (element, m-tile) tasks; it forms its
+    // kappa = 28k + g (derivative-major, one padding slot per derivative).  Each warp owns (element, m-tile) tasks; it forms its
     // A fragments (W values) in registers from the per-Gauss-point D^{blk}
     // records and the gradient table, and takes B = Phi from shared memory.
     {
@@ -593,17 +605,17 @@ __global__ void __launch_bounds__(256, 2) fe_mixed_kernel(KParams P) {
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
             const int kap = 16 * kt + 2 * tq + (j & 1) + (j >= 2 ? 8 : 0);
-            const int g = kap / 3, k = kap % 3;
-            const bool kv = kap < 3 * NG;
+            const int k = kap / 28, g = kap % 28;
+            const bool kv = kap < C::KAP && g < NG;
             float w0 = 0.f, w1 = 0.f;
             if (kv && v0) {
               const float* dt = &r32[g * C::REC32 + blk0 * 9 + k * 3];
-              const float* ph = &s_phi32[g * 3 * NPE + b0];
+              const float* ph = &s_phi32[g * C::PHS + b0];
               w0 = dt[0] * ph[0] + dt[1] * ph[NPE] + dt[2] * ph[2 * NPE];
             }
             if (kv && v1) {
               const float* dt = &r32[g * C::REC32 + blk1 * 9 + k * 3];
-              const float* ph = &s_phi32[g * 3 * NPE + b1];
+              const float* ph = &s_phi32[g * C::PHS + b1];
               w1 = dt[0] * ph[0] + dt[1] * ph[NPE] + dt[2] * ph[2 * NPE];
             }
             wv[0][j] = w0;
@@ -641,11 +653,17 @@ __global__ void __launch_bounds__(256, 2) fe_mixed_kernel(KParams P) {
             const int na = nd[a], nb = nd[b];
             const uint16_t tab_ab = tab[a * NR + b];
             const size_t p1 = (size_t)P.uu_row_ptr[(size_t)m * nu + na] + (size_t)n * P.wu[na] + (tab_ab & 0x7fff);
-            P.vals_uu[p1] = (tab_ab & 0x8000) ? v : P.vals_uu[p1] + v;
+            if (tab_ab & 0x8000)
+              P.vals_uu[p1] = v;
+            else
+              atomicAdd(&P.vals_uu[p1], v);
             if (!(m == n && a == b)) {
               const uint16_t tab_ba = tab[b * NR + a];
               const size_t p2 = (size_t)P.uu_row_ptr[(size_t)n * nu + nb] + (size_t)m * P.wu[nb] + (tab_ba & 0x7fff);
-              P.vals_uu[p2] = (tab_ba & 0x8000) ? v : P.vals_uu[p2] + v;
+              if (tab_ba & 0x8000)
+                P.vals_uu[p2] = v;
+              else
+                atomicAdd(&P.vals_uu[p2], v);
             }
           }
       }
