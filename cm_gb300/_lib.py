@@ -62,6 +62,7 @@ SIGNATURES = {
     "fe_element_residuals": [_vp, _vp, _i32, _i32, _vp, _vp],
     "fe_element_jacobians": [_vp, _vp, _i32, _i32, _vp, _vp],
     "fe_set_high_precision": [_vp, _i32],
+    "fe_set_surface_pressure": [_vp, _vp],
     "fe_check": [_vp, _vp],
     "fe_launch_count": [_vp, C.POINTER(_i64)],
     "fe_last_error": [C.c_char_p, _i32],

@@ -53,6 +53,10 @@ struct HostSetup {
   std::vector<int32_t> elem_table;       // [ne]
   std::vector<double> geo;               // [ne][NG][10]: dXi/dNu (row-major) and J_x
   std::vector<double> gbf_u, gbf_p, gw;  // quadrature tables
+  // elements with at least one boundary face, grouped by colour, and a mask of
+  // their boundary local faces (reference local-face order)
+  std::vector<int32_t> bnd_elems, bnd_ptr;
+  std::vector<uint8_t> bnd_mask;
 };
 
 // Arguments of the element kernels (plain data; device pointers).
@@ -82,6 +86,8 @@ struct KParams {
   float* vals_uu;    // FP32 uu values (mixed)
   double* elem_out;  // element-level output
   int res_only;      // mixed kernel: residual only (no Jacobian blocks)
+  int nr, pmode;     // local row nodes per element, pressure interpolation
+  const double* surf_p;  // surface pressure values [3][nu] (surface kernel)
   unsigned* status;
 };
 
@@ -89,6 +95,12 @@ struct KParams {
 // with the high-precision phases in FP64 or in double-float arithmetic.
 // Returns a cudaError_t value.
 int launch_mixed(const HostSetup& s, const KParams& kp, int num_sms, void* stream, bool double_float);
+
+// Launches the surface-pressure kernel over boundary elements (fe_surface.cu):
+// mode 0 adds into the CSR values / residual, mode 1 into element outputs.
+// Returns a cudaError_t value.
+int launch_surface(const HostSetup& s, const KParams& kp, const int32_t* belems, const uint8_t* bmask, int nb,
+                   int mode, int want_jac, int num_sms, void* stream);
 
 // Builds the set-up; returns FE_NO_ERROR or a FE_ERR_* code with msg filled.
 int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg);

@@ -473,6 +473,10 @@ struct fe_equations_set {
   uint16_t* d_tables = nullptr;
   double *d_geo = nullptr, *d_mat = nullptr, *d_gbf_u = nullptr, *d_gbf_p = nullptr, *d_gw = nullptr;
   float* d_geo_dd = nullptr;
+  double* d_surfp = nullptr;
+  int32_t* d_bnd_elems = nullptr;
+  uint8_t* d_bnd_mask = nullptr;
+  bool has_surfp = false;
   int high_precision = FE_HIGH_PRECISION_FP64;
   unsigned* d_status = nullptr;
   // staging for calls given host memory
@@ -527,6 +531,9 @@ KParams base_params(fe_handle h) {
   k.elem_p = h->d_elem_p;
   k.geo = h->d_geo;
   k.geo_dd = h->d_geo_dd;
+  k.nr = s.nr;
+  k.pmode = s.pmode;
+  k.surf_p = h->d_surfp;
   k.mat = h->d_mat;
   k.gbf_u = h->d_gbf_u;
   k.gbf_p = h->d_gbf_p;
@@ -542,6 +549,20 @@ KParams base_params(fe_handle h) {
   return k;
 }
 
+// Surface-pressure contributions of the boundary elements of colour c, after
+// that colour's volume kernel (no-op without surface pressure).
+int surface_after(fe_handle h, const KParams& kp, int c, int want_jac, cudaStream_t st) {
+  const auto& s = h->hs;
+  if (!h->has_surfp) return FE_NO_ERROR;
+  const int nb = s.bnd_ptr[c + 1] - s.bnd_ptr[c];
+  if (nb == 0) return FE_NO_ERROR;
+  const int e = cmfe::launch_surface(s, kp, h->d_bnd_elems + s.bnd_ptr[c], h->d_bnd_mask, nb, 0, want_jac,
+                                     h->num_sms, st);
+  if (e != 0) return set_error(FE_ERR_CUDA, std::string("surface kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+  h->launches++;
+  return FE_NO_ERROR;
+}
+
 // Colour-by-colour launches over all elements.
 template <int MODE>
 int run_colours(fe_handle h, KParams kp, cudaStream_t st) {
@@ -551,6 +572,7 @@ int run_colours(fe_handle h, KParams kp, cudaStream_t st) {
     kp.count = s.colour_ptr[c + 1] - s.colour_ptr[c];
     int rc = launch<MODE>(h, kp, st);
     if (rc) return rc;
+    if ((rc = surface_after(h, kp, c, MODE == M_JAC, st))) return rc;
   }
   return FE_NO_ERROR;
 }
@@ -654,6 +676,7 @@ int fe_create(const fe_mesh_desc* desc, fe_handle* out) {
     }
     if ((rc = dev_upload(&h->d_geo_dd, gdd))) return fail(rc);
   }
+  if ((rc = dev_upload(&h->d_bnd_elems, s.bnd_elems)) || (rc = dev_upload(&h->d_bnd_mask, s.bnd_mask))) return fail(rc);
   if (cudaMalloc(&h->d_status, sizeof(unsigned)) != cudaSuccess ||
       cudaMemset(h->d_status, 0, sizeof(unsigned)) != cudaSuccess)
     return fail(set_error(FE_ERR_CUDA, "status allocation failed"));
@@ -663,7 +686,7 @@ int fe_create(const fe_mesh_desc* desc, fe_handle* out) {
 
 int fe_destroy(fe_handle h) {
   if (!h) return FE_NO_ERROR;
-  void* ptrs[] = {h->d_geo_dd, h->d_elem_u, h->d_elem_p, h->d_row_ptr, h->d_uu_row_ptr, h->d_cp_row_ptr, h->d_wu,
+  void* ptrs[] = {h->d_surfp, h->d_bnd_elems, h->d_bnd_mask, h->d_geo_dd, h->d_elem_u, h->d_elem_p, h->d_row_ptr, h->d_uu_row_ptr, h->d_cp_row_ptr, h->d_wu,
                   h->d_wp, h->d_elem_table, h->d_colour_elems, h->d_tables, h->d_geo, h->d_mat,
                   h->d_gbf_u, h->d_gbf_p, h->d_gw, h->d_status, h->s_x, h->s_r, h->s_vals, h->s_cp,
                   h->s_uu, h->s_elem};
@@ -748,6 +771,7 @@ int fe_residual_evaluate(fe_handle h, const double* x, double* r, void* stream) 
     const int e = cmfe::launch_mixed(h->hs, kp, h->num_sms, st, h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT);
     if (e != 0) return set_error(FE_ERR_CUDA, std::string("residual kernel launch: ") + cudaGetErrorString((cudaError_t)e));
     h->launches++;
+    if ((rc = surface_after(h, kp, c, 0, st))) return rc;
   }
   if (hr) {
     CUDA_TRY(cudaMemcpyAsync(r, dr, sizeof(double) * h->hs.ndofs, cudaMemcpyDeviceToHost, st));
@@ -826,6 +850,7 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
     const int e = cmfe::launch_mixed(h->hs, kp, h->num_sms, st, h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT);
     if (e != 0) return set_error(FE_ERR_CUDA, std::string("mixed kernel launch: ") + cudaGetErrorString((cudaError_t)e));
     h->launches++;
+    if ((rc = surface_after(h, kp, c, 1, st))) return rc;
   }
   if (hu) CUDA_TRY(cudaMemcpyAsync(values_uu, du, sizeof(float) * h->hs.nnz_uu, cudaMemcpyDeviceToHost, st));
   if (hc) CUDA_TRY(cudaMemcpyAsync(values_coupling, dc, sizeof(double) * h->hs.nnz_cp, cudaMemcpyDeviceToHost, st));
@@ -867,6 +892,12 @@ static int element_eval(fe_handle h, const double* x, int32_t first, int32_t cou
   kp.count = count;
   kp.elems = nullptr;
   if ((rc = jac ? launch<M_EJAC>(h, kp, st) : launch<M_ERES>(h, kp, st))) return rc;
+  if (h->has_surfp && !h->hs.bnd_elems.empty()) {
+    const int e = cmfe::launch_surface(h->hs, kp, h->d_bnd_elems, h->d_bnd_mask, (int)h->hs.bnd_elems.size(), 1,
+                                       jac ? 1 : 0, h->num_sms, st);
+    if (e != 0) return set_error(FE_ERR_CUDA, std::string("surface kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+    h->launches++;
+  }
   if (ho) {
     CUDA_TRY(cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, st));
     return finish_status(h, st);
@@ -880,6 +911,21 @@ int fe_element_residuals(fe_handle h, const double* x, int32_t first, int32_t co
 
 int fe_element_jacobians(fe_handle h, const double* x, int32_t first, int32_t count, double* out, void* stream) {
   return element_eval(h, x, first, count, out, stream, true);
+}
+
+int fe_set_surface_pressure(fe_handle h, const double* values) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(h->mu);
+  if (!values) {
+    h->has_surfp = false;
+    return FE_NO_ERROR;
+  }
+  const size_t bytes = sizeof(double) * 3 * (size_t)h->hs.nu;
+  if ((rc = ensure((void**)&h->d_surfp, bytes))) return rc;
+  CUDA_TRY(cudaMemcpy(h->d_surfp, values, bytes, cudaMemcpyDefault));
+  h->has_surfp = true;
+  return FE_NO_ERROR;
 }
 
 int fe_set_high_precision(fe_handle h, int32_t mode) {

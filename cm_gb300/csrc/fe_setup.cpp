@@ -25,6 +25,8 @@
 //     :3883-4149).  The geometry does not change during a solve, so it is
 //     computed here once.
 #include <algorithm>
+#include <array>
+#include <map>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -384,6 +386,44 @@ int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg) {
       }
     }
     s.ntables = (int)seen.size();
+  }
+
+  // Boundary faces: a local face (reference order -xi1, -xi2, -xi3, +xi1,
+  // +xi2, +xi3) whose four corner nodes no other element holds.
+  {
+    auto corners = [&](int e, int lf, std::array<int32_t, 4>& c4) {
+      const int ni = lf % 3, side = lf / 3, xa = ni == 0 ? 1 : 0, xb = ni == 2 ? 1 : 2, n1 = s.n1;
+      int k = 0;
+      for (int f2 = 0; f2 < 2; ++f2)
+        for (int f1 = 0; f1 < 2; ++f1) {
+          int pos[3];
+          pos[ni] = side ? n1 - 1 : 0;
+          pos[xa] = f1 ? n1 - 1 : 0;
+          pos[xb] = f2 ? n1 - 1 : 0;
+          c4[k++] = unode(e, pos[0] + n1 * (pos[1] + n1 * pos[2]));
+        }
+      std::sort(c4.begin(), c4.end());
+    };
+    std::map<std::array<int32_t, 4>, int> count;
+    std::array<int32_t, 4> c4;
+    for (int e = 0; e < s.ne; ++e)
+      for (int lf = 0; lf < 6; ++lf) {
+        corners(e, lf, c4);
+        ++count[c4];
+      }
+    s.bnd_mask.assign(s.ne, 0);
+    for (int e = 0; e < s.ne; ++e)
+      for (int lf = 0; lf < 6; ++lf) {
+        corners(e, lf, c4);
+        if (count[c4] == 1) s.bnd_mask[e] |= (uint8_t)(1u << lf);
+      }
+    s.bnd_ptr.assign(s.ncolours + 1, 0);
+    s.bnd_elems.clear();
+    for (int c = 0; c < s.ncolours; ++c) {
+      for (int i = s.colour_ptr[c]; i < s.colour_ptr[c + 1]; ++i)
+        if (s.bnd_mask[s.colour_elems[i]]) s.bnd_elems.push_back(s.colour_elems[i]);
+      s.bnd_ptr[c + 1] = (int32_t)s.bnd_elems.size();
+    }
   }
 
   // Quadrature tables.

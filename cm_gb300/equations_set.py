@@ -162,6 +162,16 @@ class FiniteElasticityEquationsSet:
         return out.reshape(count, n, n).transpose(1, 2) if not isinstance(out, np.ndarray) else \
             out.reshape(count, n, n).transpose(0, 2, 1)
 
+    def set_surface_pressure(self, values):
+        """Nodal surface pressure [3][nu] (component n loads the boundary faces
+        normal to xi_n), as numpy or CUDA tensor; None removes the load."""
+        if values is None:
+            check(_lib.load().fe_set_surface_pressure(self._h, None))
+            return
+        if isinstance(values, np.ndarray):
+            values = np.ascontiguousarray(values, dtype=np.float64)
+        check(_lib.load().fe_set_surface_pressure(self._h, _ptr(values)))
+
     def set_high_precision(self, mode: str):
         """'fp64' (IEEE binary64, default) or 'double_float' (FP32 pairs, about
         48 significant bits) for the residual and pressure-coupling parts of

@@ -136,6 +136,15 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
 int fe_mixed_layout(fe_handle h, int64_t* nnz_uu, int64_t* nnz_coupling, int32_t* uu_row_ptr,
                     int32_t* cp_row_ptr);
 
+/* Surface-pressure follower load (FiniteElasticity_SurfacePressure{Residual,
+ * Jacobian}Evaluate, finite_elasticity_routines.f90:3215-3361, :3049-3208):
+ * values holds [3][num_nodes_u] nodal pressures, component n loading the
+ * boundary faces normal to xi_n (the reference's pressure-values parameter set
+ * of the DELUDELN variable).  Faces whose nodal values are all zero carry no
+ * load.  Host or device memory; copied.  NULL removes the load.  Applies to
+ * every later residual and Jacobian evaluation. */
+int fe_set_surface_pressure(fe_handle h, const double* values);
+
 /* Arithmetic of the high-precision parts of fe_residual_evaluate and
  * fe_jacobian_evaluate_mixed (the residual and the displacement-pressure
  * coupling blocks).  FE_HIGH_PRECISION_FP64 (the default) uses IEEE binary64.

@@ -83,6 +83,9 @@ struct OrProblem {
   const double* X;          // geometric field, [3][nu] component-major
   const double* mat;        // [nmat] or [ne][nmat]
   const double* fibre;      // nullable: fibre field angles [3][nu] (radians)
+  const double* surf_p;     // nullable: surface pressure values [3][nu]; component n loads
+                            // faces normal to xi_n (FIELD_PRESSURE_VALUES_SET_TYPE of DELUDELN)
+  const uint8_t* bface;     // [ne][6] boundary-face flags (or_boundary_faces), needed with surf_p
 };
 
 }  // extern "C"
@@ -524,9 +527,158 @@ void gp_kinematics(const OrProblem* P, const Elem& E, int g, GP& G) {
   G.Jznu = G.dep.jac / G.geo.jac;
 }
 
+// Local faces in the reference's order (basis_routines.f90:2162-2224): the
+// -xi faces for xi = 1,2,3, then the +xi faces.  Face nodes run along the
+// first in-face direction fastest (OTHER_XI_DIRECTIONS3, constants.f90:270):
+// normal xi1 -> (xi2, xi3), xi2 -> (xi1, xi3), xi3 -> (xi1, xi2).
+void face_info(int lf, int n1, int& ni, int& side, int& xa, int& xb, int nodes[9]) {
+  ni = lf % 3;
+  side = lf / 3;
+  xa = ni == 0 ? 1 : 0;
+  xb = ni == 2 ? 1 : 2;
+  for (int f2 = 0; f2 < n1; ++f2)
+    for (int f1 = 0; f1 < n1; ++f1) {
+      int pos[3];
+      pos[ni] = side ? n1 - 1 : 0;
+      pos[xa] = f1;
+      pos[xb] = f2;
+      nodes[f1 + n1 * f2] = pos[0] + n1 * (pos[1] + n1 * pos[2]);
+    }
+}
+
+// Face quadrature tables: 3x3 Gauss-Legendre on the face, point ng = i + 3j.
+struct FaceTab {
+  double w[9], N[9][9], dN[9][2][9];
+};
+const FaceTab& face_tab(int n1) {
+  static FaceTab t[2];
+  static bool init = false;
+  if (!init) {
+    double gx[3], gw[3];
+    gauss_legendre3(gx, gw);
+    for (int k = 0; k < 2; ++k) {
+      const int m = k + 2;
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) {
+          const int ng = i + 3 * j;
+          t[k].w[ng] = gw[i] * gw[j];
+          for (int f2 = 0; f2 < m; ++f2)
+            for (int f1 = 0; f1 < m; ++f1) {
+              const int f = f1 + m * f2;
+              t[k].N[ng][f] = 1.0 * lagrange(m, f1 + 1, 0, gx[i]) * lagrange(m, f2 + 1, 0, gx[j]);
+              t[k].dN[ng][0][f] = 1.0 * lagrange(m, f1 + 1, 1, gx[i]) * lagrange(m, f2 + 1, 0, gx[j]);
+              t[k].dN[ng][1][f] = 1.0 * lagrange(m, f1 + 1, 0, gx[i]) * lagrange(m, f2 + 1, 1, gx[j]);
+            }
+        }
+    }
+    init = true;
+  }
+  return t[n1 - 2];
+}
+
+// FiniteElasticity_SurfacePressureResidualEvaluate (finite_elasticity_routines.f90:3215-3361) when re,
+// FiniteElasticity_SurfacePressureJacobianEvaluate (:3049-3208) when Ke (column-major, lower
+// off-diagonal displacement blocks only, before the element matrix is mirrored).
+void surface_pressure(const OrProblem* P, int e, const Elem& E, double* re, double* Ke, int n) {
+  if (!P->surf_p || !P->bface) return;
+  const int n1 = P->nxi_u, nf = n1 * n1, npe = E.npe;
+  const FaceTab& T = face_tab(n1);
+  static const int ORIENT[3] = {1, -1, 1};  // OTHER_XI_ORIENTATIONS3 of the in-face pair
+  for (int lf = 0; lf < 6; ++lf) {
+    if (!P->bface[(size_t)e * 6 + lf]) continue;
+    int ni, side, xa, xb, fn[9];
+    face_info(lf, n1, ni, side, xa, xb, fn);
+    double pf[9];
+    bool nonzero = false;
+    for (int f = 0; f < nf; ++f) {
+      pf[f] = P->surf_p[(size_t)ni * P->nu + P->elem_u[(size_t)e * npe + fn[f]]];
+      if (std::fabs(pf[f]) > ZERO_TOLERANCE) nonzero = true;
+    }
+    if (!nonzero) continue;
+    const int orientation = (side ? 1 : -1) * ORIENT[ni] > 0 ? 1 : -1;
+    for (int ng = 0; ng < 9; ++ng) {
+      double p = 0.0, g[3][2];
+      for (int f = 0; f < nf; ++f) p = p + T.N[ng][f] * pf[f];
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 2; ++d) {
+          double s = 0.0;
+          for (int f = 0; f < nf; ++f) s = s + T.dN[ng][d][f] * E.z[fn[f]][c];
+          g[c][d] = s;
+        }
+      // COORDINATE_METRICS_CALCULATE, surface in 3-D space (coordinate_routines.f90:908-915)
+      double GL[2][2];
+      for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) GL[a][b] = g[0][a] * g[0][b] + g[1][a] * g[1][b] + g[2][a] * g[2][b];
+      const double det_gl = GL[0][0] * GL[1][1] - GL[1][0] * GL[0][1];
+      double dxi[2][3];
+      for (int c = 0; c < 3; ++c) {
+        dxi[0][c] = (GL[1][1] * g[c][0] - GL[0][1] * g[c][1]) / det_gl;
+        dxi[1][c] = (GL[0][0] * g[c][1] - GL[1][0] * g[c][0]) / det_gl;
+      }
+      double a1[3] = {g[0][0], g[1][0], g[2][0]}, a2[3] = {g[0][1], g[1][1], g[2][1]}, nrm[3];
+      cross3(a1, a2, nrm);
+      const double pg = p * orientation;
+      const double gwp = T.w[ng] * pg;
+      if (re) {
+        for (int c = 0; c < 3; ++c) {
+          const double gpn = gwp * nrm[c];
+          for (int f = 0; f < nf; ++f) re[c * npe + fn[f]] = re[c * npe + fn[f]] + gpn * T.N[ng][f];
+        }
+      }
+      if (Ke) {
+        static const int OD[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+        for (int oh = 0; oh < 3; ++oh) {
+          const int nh = OD[oh][0], mh = OD[oh][1];
+          double W[2];
+          for (int i = 0; i < 2; ++i) W[i] = (nrm[mh] * dxi[i][nh] - dxi[i][mh] * nrm[nh]) * gwp;
+          for (int ns = 0; ns < nf; ++ns) {
+            const double t1[2] = {W[0] * T.dN[ng][0][ns], W[1] * T.dN[ng][1][ns]};
+            const int col = nh * npe + fn[ns];
+            for (int ms = 0; ms < nf; ++ms) {
+              const double t2 = T.N[ng][ms];
+              const int row = mh * npe + fn[ms];
+              Ke[(size_t)col * n + row] = Ke[(size_t)col * n + row] + (t1[0] * t2 + t1[1] * t2);
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+// Boundary faces: a local face whose corner nodes no other element holds
+// (DECOMPOSITION face BOUNDARY_FACE).  flags has [ne][6] entries.
+void or_boundary_faces(const OrProblem* P, uint8_t* flags) {
+  const int n1 = P->nxi_u, npe = n1 * n1 * n1;
+  std::vector<std::vector<int>> surr(P->nu);
+  for (int e = 0; e < P->ne; ++e)
+    for (int a = 0; a < npe; ++a) surr[P->elem_u[(size_t)e * npe + a]].push_back(e);
+  for (int e = 0; e < P->ne; ++e)
+    for (int lf = 0; lf < 6; ++lf) {
+      int ni, side, xa, xb, fn[9];
+      face_info(lf, n1, ni, side, xa, xb, fn);
+      const int nf = n1 * n1;
+      int corners[4] = {P->elem_u[(size_t)e * npe + fn[0]], P->elem_u[(size_t)e * npe + fn[n1 - 1]],
+                        P->elem_u[(size_t)e * npe + fn[nf - n1]], P->elem_u[(size_t)e * npe + fn[nf - 1]]};
+      bool shared = false;
+      for (int f : surr[corners[0]]) {
+        if (f == e) continue;
+        int hit = 0;
+        for (int k = 0; k < 4; ++k)
+          for (int a = 0; a < npe; ++a)
+            if (P->elem_u[(size_t)f * npe + a] == corners[k]) {
+              ++hit;
+              break;
+            }
+        if (hit == 4) shared = true;
+      }
+      flags[(size_t)e * 6 + lf] = shared ? 0 : 1;
+    }
+}
 
 // Number of element rows (3*npe_u + npe_p).
 int or_element_size(const OrProblem* P) {
@@ -577,6 +729,7 @@ void or_element_residual(const OrProblem* P, int e, const double* x, double* re)
       re[mhs] = re[mhs] + t1;
     }
   }
+  surface_pressure(P, e, E, re, nullptr, E.nrow);
 }
 
 // FiniteElasticity_FiniteElementJacobianEvaluate (finite_elasticity_routines.f90:842-1175),
@@ -662,6 +815,8 @@ void or_element_jacobian(const OrProblem* P, int e, const double* x, double* Ke)
         }
       }
   }
+  // surface pressure follower load before the mirror (:1075-1078)
+  surface_pressure(P, e, E, nullptr, Ke, n);
   // mirror the lower triangle (:1149-1153)
   for (int c = 1; c < n; ++c)
     for (int r = 0; r < c; ++r) K(r, c) = K(c, r);

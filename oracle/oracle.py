@@ -25,7 +25,7 @@ class OrProblem(C.Structure):
         ("ne", C.c_int32), ("nu", C.c_int32), ("np", C.c_int32), ("nxi_u", C.c_int32),
         ("p_mode", C.c_int32), ("law", C.c_int32), ("nmat", C.c_int32), ("mat_per_element", C.c_int32),
         ("elem_u", C.c_void_p), ("elem_p", C.c_void_p), ("X", C.c_void_p), ("mat", C.c_void_p),
-        ("fibre", C.c_void_p),
+        ("fibre", C.c_void_p), ("surf_p", C.c_void_p), ("bface", C.c_void_p),
     ]
 
 
@@ -50,6 +50,7 @@ def lib():
         L.or_regular_mesh.argtypes = [C.c_int] * 4 + [vp, vp]; L.or_regular_mesh.restype = C.c_int
         L.or_basis_tables.argtypes = [C.c_int, vp, vp, vp]
         L.or_point_stress.argtypes = [C.c_int, vp, vp, C.c_double, C.c_double, vp, vp]
+        L.or_boundary_faces.argtypes = [P, vp]
         _lib = L
     return _lib
 
@@ -80,6 +81,24 @@ class Problem:
                                                   _p(self.mat), _p(self.fibre))
         self.s = s
         self.ref = C.byref(s)
+        self.surf_p = None
+        self.bface = None
+        sp = getattr(mesh, "surface_pressure", None)
+        if sp is not None:
+            self.set_surface_pressure(sp)
+
+    def set_surface_pressure(self, values):
+        """values: [3][nu] nodal pressure (component n loads faces normal to xi_n), or None."""
+        if values is None:
+            self.surf_p = None
+            self.s.surf_p = None
+            return
+        self.surf_p = np.ascontiguousarray(values, dtype=np.float64).reshape(3, self.m.nu)
+        if self.bface is None:
+            self.bface = np.zeros((self.m.ne, 6), dtype=np.uint8)
+            lib().or_boundary_faces(self.ref, self.bface.ctypes.data)
+        self.s.surf_p = self.surf_p.ctypes.data
+        self.s.bface = self.bface.ctypes.data
 
     @property
     def nrow(self):

@@ -240,3 +240,57 @@ def test_native_library_launches(torch):
     es.jacobian_evaluate(torch.from_numpy(state(m)).cuda())
     torch.cuda.synchronize()
     assert es.launch_count() - before >= 8  # one launch per element colour
+
+
+def pressure_meshes():
+    out = {}
+    for name, nxi, pm, law, mats, fib in [
+            ("quad_node_mr", 3, "node", M.MR, (2.0, 6.0), None),
+            ("lin_elem_mr", 2, "element", M.MR, (2.0, 6.0), None),
+            ("quad_node_guccione_fibres", 3, "node", M.GUCCIONE, (0.88, 18.5, 3.58, 1.63),
+             np.array([[-0.5], [0.0], [0.0]]))]:
+        m = M.regular_box(3, 2, 2, lengths=(4.0, 3.0, 2.0), nxi_u=nxi, pressure=pm, law=law, materials=mats,
+                          perturb=0.05, seed=6, fibre=fib)
+        sp = np.zeros((3, m.nu))
+        i, j, k = m.node_ijk()
+        sp[2, k == 0] = 1.2 * (1.0 + 0.3 * i[k == 0] / i.max())   # z = 0 faces (normal xi3)
+        sp[0, i == i.max()] = -0.4                                 # x = max faces (normal xi1)
+        out[name] = (m, sp)
+    return out
+
+
+@pytest.mark.parametrize("name", list(pressure_meshes()))
+def test_surface_pressure_parity(torch, oracle, name):
+    m, sp = pressure_meshes()[name]
+    x = state(m)
+    P = oracle.Problem(m)
+    P.set_surface_pressure(sp)
+    rp_o, col_o = P.pattern()
+    vo, ro = P.assemble(x, rp_o, col_o, nthreads=1)
+    es = FiniteElasticityEquationsSet(m)
+    es.set_surface_pressure(sp)
+    xd = torch.from_numpy(x).cuda()
+    # element level
+    K = es.element_jacobians(xd).cpu().numpy()
+    R = es.element_residuals(xd).cpu().numpy()
+    for e in range(m.ne):
+        assert_entrywise(K[e], P.element_jacobian(e, x), what="%s K_e[%d]" % (name, e))
+        assert_entrywise(R[e], P.element_residual(e, x), what="%s r_e[%d]" % (name, e))
+    # assembled, FP64
+    r = torch.empty_like(xd)
+    v = es.jacobian_evaluate(xd, r=r)
+    assert_entrywise(v.cpu().numpy(), vo, what=name + " CSR values")
+    assert_entrywise(r.cpu().numpy(), ro, what=name + " residual")
+    assert_entrywise(es.residual_evaluate(xd).cpu().numpy(), ro, what=name + " residual-only")
+    # assembled, mixed
+    rm = torch.empty_like(xd)
+    vu, vc = es.jacobian_evaluate_mixed(xd, r=rm)
+    es.check_status(xd)
+    full = es.mixed_to_full(vu.cpu().numpy(), vc.cpu().numpy())
+    assert np.abs(full - vo).max() < MIXED_UU_TOL * np.abs(vo).max()
+    assert_entrywise(rm.cpu().numpy(), ro, what=name + " mixed residual")
+    # removing the load restores the unloaded result
+    es.set_surface_pressure(None)
+    P0 = oracle.Problem(m)
+    _, r0 = P0.assemble(x, rp_o, col_o, jacobian=False)
+    assert_entrywise(es.residual_evaluate(xd).cpu().numpy(), r0, what=name + " unloaded")

@@ -250,3 +250,65 @@ def test_abi_exports_every_declared_symbol():
     for n in names:
         assert hasattr(L, n), n
         assert n in _lib.SIGNATURES, n
+
+
+def _pressure_mesh(nxi, pmode, p0=1.5):
+    m = M.regular_box(2, 2, 1, lengths=(2.0, 2.0, 1.0), nxi_u=nxi, pressure=pmode, law=M.MR,
+                      materials=(2.0, 6.0), perturb=0.05, seed=4)
+    sp = np.zeros((3, m.nu))
+    i, j, k = m.node_ijk()
+    sp[2, k == 0] = p0 * (1.0 + 0.2 * i[k == 0] / i.max())  # load on the z = 0 faces (normal xi3)
+    return m, sp
+
+
+@pytest.mark.parametrize("nxi,pmode", [(2, "element"), (3, "node")])
+def test_surface_pressure_total_force(oracle, nxi, pmode):
+    """Uniform pressure p on the flat z = 0 face of the undeformed box: the
+    surface part of the residual sums to p times the face area along the
+    outward normal (-z), and has no in-plane resultant."""
+    m = M.regular_box(2, 2, 1, lengths=(2.0, 3.0, 1.0), nxi_u=nxi, pressure=pmode)
+    x = np.concatenate([m.X.ravel(), np.zeros(m.n_pressure)])
+    P = oracle.Problem(m)
+    rp, col = P.pattern()
+    _, r0 = P.assemble(x, rp, col, jacobian=False)
+    sp = np.zeros((3, m.nu))
+    i, j, k = m.node_ijk()
+    sp[2, k == 0] = 0.7  # faces normal to xi3 with nonzero nodal pressure: the z = 0 faces only
+    P.set_surface_pressure(sp)
+    _, r1 = P.assemble(x, rp, col, jacobian=False)
+    d = r1 - r0
+    nu = m.nu
+    assert abs(d[2 * nu:3 * nu].sum() - (-0.7 * 6.0)) < 1e-12
+    assert abs(d[:nu].sum()) < 1e-12 and abs(d[nu:2 * nu].sum()) < 1e-12
+    assert np.all(d[2 * nu:3 * nu][k > 0] == 0.0)
+
+
+@pytest.mark.parametrize("nxi,pmode", [(2, "element"), (3, "node")])
+def test_surface_pressure_tangent_matches_fd_on_lower_blocks(oracle, nxi, pmode):
+    """The follower-load tangent is computed for the lower displacement blocks
+    and mirrored (finite_elasticity_routines.f90:1075-1078, :1149-1153), so the
+    analytic element Jacobian equals the central-difference derivative of the
+    residual on every entry except the mirrored upper off-diagonal blocks."""
+    m, sp = _pressure_mesh(nxi, pmode)
+    x = M.deformed_state(m, stretch=1.05, shear=0.03, noise=0.03, pressure=-1.0, seed=8)
+    P = oracle.Problem(m)
+    P.set_surface_pressure(sp)
+    npe = nxi ** 3
+    for e in range(m.ne):
+        K = P.element_jacobian(e, x)
+        dofs = P.element_dofs(e)
+        Kc = np.zeros_like(K)
+        h = 1e-6
+        for jj, d in enumerate(dofs):
+            xp, xm = x.copy(), x.copy()
+            xp[d] += h
+            xm[d] -= h
+            Kc[:, jj] = (P.element_residual(e, xp) - P.element_residual(e, xm)) / (2 * h)
+        n = K.shape[0]
+        comp = np.minimum(np.arange(n) // npe, 3)
+        mask = ~((comp[:, None] < comp[None, :]) & (comp[:, None] < 3) & (comp[None, :] < 3))
+        err = np.abs(K - Kc)[mask].max() / np.abs(K).max()
+        assert err < 1e-7, (e, err)
+    # the surface term is present: the element Jacobian changes with the load
+    P2 = oracle.Problem(m)
+    assert np.abs(P.element_jacobian(0, x) - P2.element_jacobian(0, x)).max() > 1e-3
