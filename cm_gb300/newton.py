@@ -1,0 +1,377 @@
+"""Load-stepped Newton solve on the GPU around the assembly library.
+
+Restates the reference's solve path for the static finite-elasticity problem
+(the control loop and SNES settings the assembly path is called from):
+
+* load increments — PROBLEM_CONTROL_LOAD_INCREMENT_LOOP (problem_routines.f90:
+  643-691) with EQUATIONS_SET_BOUNDARY_CONDITIONS_INCREMENT
+  (equations_set_routines.f90:6491-6590): every fixed-incremented Dirichlet
+  value moves as NEW = CUR + (FULL - CUR)/(N - i + 1), and takes exactly FULL
+  on the last increment;
+* Newton — SOLVER_NEWTON_LINESEARCH defaults (solver_routines.f90:17803-17812,
+  18772-18775): initial guess = the current field, at most 50 iterations,
+  cubic backtracking line search with alpha = 1e-4 and maximum step 1e8, and
+  the absolute residual tolerance 1e-10 (the convergence test here is
+  ||r||_2 <= atol on the free dofs);
+* solver mapping — rows and columns of Dirichlet dofs are removed from the
+  linear system (solver_mapping_routines.f90:1420,1592).
+
+PETSc is not part of this build: the cubic backtracking step follows the
+published Dennis-Schnabel algorithm that PETSc's "bt" line search implements,
+and the linear solve is a dense LU (small systems) or restarted GMRES with a
+block-diagonal (Jacobi / Schur-diagonal) preconditioner, both on the GPU.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+
+@dataclass
+class NewtonOptions:
+    atol: float = 1e-10          # ||r_free||_2 stopping tolerance
+    max_iterations: int = 50
+    alpha: float = 1e-4          # sufficient-decrease constant of the line search
+    max_step: float = 1e8
+    min_lambda: float = 1e-10
+    precision: str = "fp64"      # "fp64" Jacobian, or "mixed" (FP32 displacement block)
+    high_precision: str = "fp64"  # residual/coupling arithmetic of the mixed path
+    linear: str = "auto"         # "dense", "gmres" or "auto" (dense up to dense_limit free dofs)
+    dense_limit: int = 12000
+    gmres_rtol: float = 1e-6
+    gmres_restart: int = 80
+    gmres_max_iterations: int = 3000
+
+
+@dataclass
+class StepReport:
+    iterations: int = 0
+    converged: bool = False
+    residual_norms: list = field(default_factory=list)
+    linear_iterations: list = field(default_factory=list)
+    line_search_lambdas: list = field(default_factory=list)
+    seconds: float = 0.0
+    assembly_seconds: float = 0.0
+    linear_seconds: float = 0.0
+
+
+class DirichletConditions:
+    """Fixed and fixed-incremented Dirichlet values on dofs (BOUNDARY_CONDITION_FIXED and
+    BOUNDARY_CONDITION_FIXED_INCREMENTED, boundary_condition_routines.f90:100-108)."""
+
+    def __init__(self, ndofs: int):
+        self.ndofs = ndofs
+        self.dofs = np.zeros(0, dtype=np.int64)
+        self.full = np.zeros(0)
+        self.incremented = np.zeros(0, dtype=bool)
+
+    def fix(self, dofs, values, incremented=False):
+        dofs = np.asarray(dofs, dtype=np.int64).ravel()
+        values = np.broadcast_to(np.asarray(values, dtype=np.float64), dofs.shape).copy()
+        keep = ~np.isin(dofs, self.dofs)
+        self.dofs = np.concatenate([self.dofs, dofs[keep]])
+        self.full = np.concatenate([self.full, values[keep]])
+        self.incremented = np.concatenate([self.incremented, np.full(int(keep.sum()), bool(incremented))])
+        return self
+
+    def free_mask(self):
+        m = np.ones(self.ndofs, dtype=bool)
+        m[self.dofs] = False
+        return m
+
+
+class FreeDofSystem:
+    """Index maps from the full CSR pattern to the free-dof submatrix."""
+
+    def __init__(self, es, free_mask, device):
+        rp, col = es.csr_pattern(base=0)
+        n = es.ndofs
+        rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(rp))
+        keep = free_mask[rows] & free_mask[col]
+        new_index = -np.ones(n, dtype=np.int64)
+        new_index[free_mask] = np.arange(int(free_mask.sum()))
+        self.nf = int(free_mask.sum())
+        self.sel = torch.from_numpy(np.nonzero(keep)[0]).to(device)
+        r = new_index[rows[keep]]
+        c = new_index[col[keep]]
+        counts = np.bincount(r, minlength=self.nf)
+        self.crow = torch.from_numpy(np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)).to(device)
+        self.col = torch.from_numpy(c.astype(np.int64)).to(device)
+        self.row = torch.from_numpy(r.astype(np.int64)).to(device)
+        self.free = torch.from_numpy(np.nonzero(free_mask)[0]).to(device)
+        self.is_p = torch.from_numpy(np.nonzero(free_mask)[0] >= 3 * es.mesh.nu).to(device)
+        self.is_diag = (self.row == self.col)
+        self.device = device
+
+    def matrix(self, vals_full):
+        v = vals_full[self.sel]
+        return torch.sparse_csr_tensor(self.crow, self.col, v, size=(self.nf, self.nf))
+
+
+def _gmres(A, b, M, rtol, restart, max_it):
+    """Right-preconditioned restarted GMRES (FP64); M(v) applies the preconditioner."""
+    n = b.numel()
+    x = torch.zeros_like(b)
+    bnorm = float(b.norm())
+    if bnorm == 0.0:
+        return x, 0
+    total = 0
+    r = b.clone()
+    while total < max_it:
+        beta = float(r.norm())
+        if beta <= rtol * bnorm:
+            break
+        V = torch.zeros(restart + 1, n, dtype=b.dtype, device=b.device)
+        Z = torch.zeros(restart, n, dtype=b.dtype, device=b.device)
+        H = torch.zeros(restart + 1, restart, dtype=torch.float64)
+        V[0] = r / beta
+        g = torch.zeros(restart + 1, dtype=torch.float64)
+        g[0] = beta
+        cs = torch.zeros(restart, dtype=torch.float64)
+        sn = torch.zeros(restart, dtype=torch.float64)
+        k = 0
+        while k < restart and total < max_it:
+            Z[k] = M(V[k])
+            w = A @ Z[k]
+            # modified Gram-Schmidt, done as one pass of classical GS plus one refinement
+            h = V[:k + 1] @ w
+            w = w - V[:k + 1].T @ h
+            h2 = V[:k + 1] @ w
+            w = w - V[:k + 1].T @ h2
+            h = (h + h2).double().cpu()
+            hn = float(w.norm())
+            H[:k + 1, k] = h
+            H[k + 1, k] = hn
+            if hn > 0:
+                V[k + 1] = w / hn
+            for i in range(k):
+                t = cs[i] * H[i, k] + sn[i] * H[i + 1, k]
+                H[i + 1, k] = -sn[i] * H[i, k] + cs[i] * H[i + 1, k]
+                H[i, k] = t
+            d = float(torch.sqrt(H[k, k] ** 2 + H[k + 1, k] ** 2))
+            cs[k], sn[k] = H[k, k] / d, H[k + 1, k] / d
+            H[k, k] = d
+            H[k + 1, k] = 0.0
+            g[k + 1] = -sn[k] * g[k]
+            g[k] = cs[k] * g[k]
+            k += 1
+            total += 1
+            if abs(float(g[k])) <= rtol * bnorm:
+                break
+        y = torch.linalg.solve_triangular(H[:k, :k], g[:k].unsqueeze(1), upper=True).squeeze(1)
+        x = x + Z[:k].T @ y.to(b.device)
+        r = b - A @ x
+    return x, total
+
+
+class LoadStepSolver:
+    """Load-stepped Newton for one equations set on the GPU."""
+
+    def __init__(self, es, bc: DirichletConditions, options: NewtonOptions | None = None, device="cuda"):
+        self.es = es
+        self.bc = bc
+        self.opt = options or NewtonOptions()
+        self.device = torch.device(device)
+        self.free_mask = bc.free_mask()
+        self.sys = FreeDofSystem(es, self.free_mask, self.device)
+        self.bc_dofs = torch.from_numpy(bc.dofs).to(self.device)
+        if self.opt.precision == "mixed":
+            es.set_high_precision(self.opt.high_precision)
+            uu_rp, cp_rp = (a.astype(np.int64) for a in es.mixed_layout())
+            rp = es.csr_pattern()[0].astype(np.int64)
+            nu3 = 3 * es.mesh.nu
+            # positions of the mixed split's entries in the full pattern: each
+            # displacement row holds its uu entries first, then its coupling entries
+            ku = np.zeros(es.ndofs, dtype=np.int64)
+            ku[:nu3] = np.diff(uu_rp)
+            ru = np.repeat(np.arange(nu3), ku[:nu3])
+            uu_pos = rp[ru] + (np.arange(uu_rp[-1]) - uu_rp[ru])
+            rc = np.repeat(np.arange(es.ndofs), np.diff(cp_rp))
+            cp_pos = rp[rc] + ku[rc] + (np.arange(cp_rp[-1]) - cp_rp[rc])
+            self.uu_pos = torch.from_numpy(uu_pos).to(self.device)
+            self.cp_pos = torch.from_numpy(cp_pos).to(self.device)
+            self.vu = torch.empty(es.nnz_uu, dtype=torch.float32, device=self.device)
+            self.vc = torch.empty(es.nnz_coupling, dtype=torch.float64, device=self.device)
+        self.vals = torch.empty(es.nnz, dtype=torch.float64, device=self.device)
+        self.r = torch.empty(es.ndofs, dtype=torch.float64, device=self.device)
+
+    def _sync(self):
+        if self.device.type == "cuda":
+            torch.cuda.synchronize(self.device)
+
+    # -------------------------------------------------------------- pieces
+    def apply_increment(self, x, i, n):
+        """Dirichlet values for increment i of n (1-based), the reference's rule."""
+        cur = x[self.bc_dofs]
+        full = torch.from_numpy(self.bc.full).to(x)
+        inc = torch.from_numpy(self.bc.incremented).to(self.device)
+        new = full.clone() if i == n else torch.where(inc, cur + (full - cur) / (n - i + 1), full)
+        x[self.bc_dofs] = new
+        return x
+
+    def residual(self, x):
+        self.es.residual_evaluate(x, self.r)
+        return self.r[self.sys.free]
+
+    def jacobian(self, x):
+        if self.opt.precision == "mixed":
+            self.es.jacobian_evaluate_mixed(x, self.vu, self.vc, self.r)
+            self.vals[self.uu_pos] = self.vu.double()
+            self.vals[self.cp_pos] = self.vc
+        else:
+            self.es.jacobian_evaluate(x, self.vals, self.r)
+        return self.sys.matrix(self.vals), self.r[self.sys.free]
+
+    def _preconditioner(self, A):
+        """Block-diagonal preconditioner: Jacobi on displacement rows, the
+        diagonal of B diag(A)^-1 B^T on pressure rows."""
+        S = self.sys
+        v = A.values()
+        diag = torch.zeros(S.nf, dtype=torch.float64, device=self.device)
+        diag.index_add_(0, S.row[S.is_diag], v[S.is_diag])
+        inv = torch.zeros_like(diag)
+        u = ~S.is_p
+        inv[u] = 1.0 / diag[u]
+        # Schur diagonal for pressure rows: sum_j B_ij^2 / A_jj over displacement columns
+        pr = S.is_p[S.row] & ~S.is_p[S.col]
+        sd = torch.zeros_like(diag)
+        sd.index_add_(0, S.row[pr], v[pr] ** 2 * inv[S.col[pr]])
+        p = S.is_p
+        inv[p] = -1.0 / torch.where(sd[p] != 0, sd[p], torch.ones_like(sd[p]))
+        return lambda w: inv * w
+
+    def linear_solve(self, A, b):
+        if self.opt.linear == "dense" or (self.opt.linear == "auto" and self.sys.nf <= self.opt.dense_limit):
+            D = A.to_dense()
+            return torch.linalg.solve(D, b), 1
+        M = self._preconditioner(A)
+        return _gmres(A, b, M, self.opt.gmres_rtol, self.opt.gmres_restart, self.opt.gmres_max_iterations)
+
+    # -------------------------------------------------------------- Newton
+    def newton(self, x, report: StepReport | None = None):
+        """Newton iterations at the current Dirichlet values (x is updated in place)."""
+        o = self.opt
+        rep = report or StepReport()
+        t_start = time.perf_counter()
+        free = self.sys.free
+        r = self.residual(x).clone()
+        fnorm = float(r.norm())
+        rep.residual_norms.append(fnorm)
+        it = 0
+        while fnorm > o.atol and it < o.max_iterations:
+            self._sync()
+            ta = time.perf_counter()
+            A, _ = self.jacobian(x)
+            self._sync()
+            tb = time.perf_counter()
+            d, lin_it = self.linear_solve(A, -r)
+            self._sync()
+            rep.assembly_seconds += tb - ta
+            rep.linear_seconds += time.perf_counter() - tb
+            rep.linear_iterations.append(int(lin_it))
+            dn = float(d.norm())
+            if dn > o.max_step:
+                d = d * (o.max_step / dn)
+            # cubic backtracking (Dennis & Schnabel): f = 1/2 ||r||^2
+            f0 = 0.5 * fnorm * fnorm
+            slope = float(r @ (A @ d))
+            if slope > 0:
+                slope = -slope
+            lam, lam_prev, f_prev = 1.0, None, None
+            x0 = x[free].clone()
+            while True:
+                x[free] = x0 + lam * d
+                rn = self.residual(x).clone()
+                f1 = 0.5 * float(rn @ rn)
+                if np.isfinite(f1) and f1 <= f0 + o.alpha * lam * slope:
+                    break
+                if lam < o.min_lambda:
+                    break
+                if lam_prev is None or not np.isfinite(f1):
+                    lt = -slope / (2.0 * (f1 - f0 - slope)) if np.isfinite(f1) else 0.1 * lam
+                else:
+                    a1 = f1 - f0 - lam * slope
+                    a2 = f_prev - f0 - lam_prev * slope
+                    den = lam - lam_prev
+                    a = (a1 / lam ** 2 - a2 / lam_prev ** 2) / den
+                    b = (-lam_prev * a1 / lam ** 2 + lam * a2 / lam_prev ** 2) / den
+                    if a == 0.0:
+                        lt = -slope / (2.0 * b)
+                    else:
+                        disc = max(b * b - 3.0 * a * slope, 0.0)
+                        lt = (-b + np.sqrt(disc)) / (3.0 * a)
+                lam_prev, f_prev = lam, f1
+                lam = float(min(max(lt, 0.1 * lam), 0.5 * lam))
+            rep.line_search_lambdas.append(lam)
+            r = rn
+            fnorm = float(r.norm())
+            rep.residual_norms.append(fnorm)
+            it += 1
+            if lam < o.min_lambda:
+                break
+        rep.iterations = it
+        rep.converged = fnorm <= o.atol
+        self._sync()
+        rep.seconds = time.perf_counter() - t_start
+        return x, rep
+
+    def solve(self, x0, increments: int, guesses=None):
+        """All load increments from state x0; guesses (optional) maps the
+        increment number to a Newton initial guess for the free dofs."""
+        x = x0.clone()
+        reports = []
+        for i in range(1, increments + 1):
+            x = self.apply_increment(x, i, increments)
+            if guesses is not None and i in guesses:
+                x[self.sys.free] = guesses[i][self.sys.free]
+            x, rep = self.newton(x)
+            reports.append(rep)
+            if not rep.converged:
+                break
+        return x, reports
+
+
+# ----------------------------------------------------------------- set-ups
+def uniaxial_symmetry_conditions(mesh, stretch):
+    """Config-1 style uniaxial extension of a box: symmetry planes x=0 (u_x),
+    y=0 (u_y), z=0 (u_z) fixed, the x = L face moved to stretch * L in x
+    (fixed-incremented).  The symmetry planes remove the rigid rotation that
+    'x=0 face fixed in x, one corner pinned' alone would leave."""
+    nu = mesh.nu
+    bc = DirichletConditions(mesh.ndofs)
+    i, j, k = mesh.node_ijk()
+    n1, n2, n3 = mesh.grid_u
+    X = mesh.X
+    bc.fix(np.nonzero(i == 0)[0], X[0, i == 0])
+    bc.fix(nu + np.nonzero(j == 0)[0], X[1, j == 0])
+    bc.fix(2 * nu + np.nonzero(k == 0)[0], X[2, k == 0])
+    right = np.nonzero(i == n1 - 1)[0]
+    bc.fix(right, stretch * X[0, right], incremented=True)
+    return bc
+
+
+def clamped_stretch_shear_conditions(mesh, stretch, shear):
+    """Config-2 style loading: the x = 0 face clamped (z = X), the x = L face
+    moved to z_x = stretch * L, z_y = Y + shear * L, z_z = Z (fixed-incremented)."""
+    nu = mesh.nu
+    bc = DirichletConditions(mesh.ndofs)
+    i, j, k = mesh.node_ijk()
+    n1 = mesh.grid_u[0]
+    X = mesh.X
+    left = np.nonzero(i == 0)[0]
+    right = np.nonzero(i == n1 - 1)[0]
+    for c in range(3):
+        bc.fix(c * nu + left, X[c, left])
+    L = X[0, right]
+    bc.fix(right, stretch * L, incremented=True)
+    bc.fix(nu + right, X[1, right] + shear * L, incremented=True)
+    bc.fix(2 * nu + right, X[2, right], incremented=True)
+    return bc
+
+
+def initial_state(mesh):
+    """The reference's initial dependent field: z = X, p = 0."""
+    return np.concatenate([mesh.X.ravel(), np.zeros(mesh.n_pressure)])

@@ -176,3 +176,40 @@ def point_stress(law, c, F, p):
     lib().or_point_stress(law, c.ctypes.data, F.ctypes.data, float(np.linalg.det(F)), float(p),
                           S.ctypes.data, Cm.ctypes.data)
     return S, Cm
+
+
+class EquationsSet:
+    """CPU equations set with the call surface of
+    ``cm_gb300.equations_set.FiniteElasticityEquationsSet`` that the Newton
+    driver uses (``csr_pattern``, ``residual_evaluate``, ``jacobian_evaluate``),
+    evaluated by the oracle.  Test infrastructure: it lets the same
+    load-stepping code run on the CPU as the checker of the GPU run."""
+
+    def __init__(self, mesh, nthreads=4):
+        self.mesh = mesh
+        self.prob = Problem(mesh)
+        self.rp1, self.col1 = self.prob.pattern()
+        self.ndofs = int(self.prob.ndofs)
+        self.nnz = int(self.rp1[-1]) - 1
+        self.nthreads = nthreads
+
+    def csr_pattern(self, base=0):
+        return (self.rp1 - 1 + base).astype(np.int32), (self.col1 - 1 + base).astype(np.int32)
+
+    def set_surface_pressure(self, values):
+        self.prob.set_surface_pressure(None if values is None else np.asarray(values))
+
+    def residual_evaluate(self, x, r):
+        _, res = self.prob.assemble(np.asarray(x), self.rp1, self.col1, jacobian=False, residual=True,
+                                    nthreads=self.nthreads)
+        r.copy_(r.new_tensor(res)) if hasattr(r, "copy_") else np.copyto(r, res)
+        return r
+
+    def jacobian_evaluate(self, x, values, r=None):
+        vals, res = self.prob.assemble(np.asarray(x), self.rp1, self.col1, jacobian=True, residual=r is not None,
+                                       nthreads=self.nthreads)
+        for dst, src in ((values, vals), (r, res)):
+            if dst is None:
+                continue
+            dst.copy_(dst.new_tensor(src)) if hasattr(dst, "copy_") else np.copyto(dst, src)
+        return values

@@ -1,0 +1,189 @@
+"""Load-stepped Newton (the caller of the assembly path).
+
+CPU tests run the driver on the oracle's equations set: the load-increment
+rule of EQUATIONS_SET_BOUNDARY_CONDITIONS_INCREMENT
+(equations_set_routines.f90:6560-6595), Newton's quadratic convergence to
+||r_free||_2 <= 1e-10, the exact discrete solution of homogeneous uniaxial
+stretch on the 4x4x4 trilinear cube, and GMRES against the dense solve.
+GPU tests run the same driver on the CUDA path (FP64 and mixed Jacobian)
+and compare every increment with the oracle run.
+"""
+import warnings
+
+import numpy as np
+import pytest
+import torch
+
+from cm_gb300 import mesh as M
+from cm_gb300 import newton as N
+
+warnings.filterwarnings("ignore", message="Sparse")
+
+
+def cube_cfg1():
+    return M.regular_box(4, 4, 4, nxi_u=2, pressure="element", law=M.MR, materials=(2.0, 6.0))
+
+
+def quad_small():
+    return M.regular_box(3, 2, 2, lengths=(1.5, 1.0, 1.0), nxi_u=3, pressure="node", law=M.MR,
+                         materials=(2.0, 6.0), perturb=0.1, seed=11)
+
+
+def oracle_solve(oracle, m, bc, increments, **opt):
+    es = oracle.EquationsSet(m)
+    s = N.LoadStepSolver(es, bc, N.NewtonOptions(**opt), device="cpu")
+    return s.solve(torch.from_numpy(N.initial_state(m)), increments)
+
+
+def test_increment_rule_reference_formula():
+    # NEW = CUR + (FULL - CUR)/(N - i + 1), FULL on the last increment
+    m = cube_cfg1()
+    bc = N.DirichletConditions(m.ndofs).fix([3, 7], [2.0, -1.0], incremented=True).fix([11], 0.5)
+
+    class _ES:
+        mesh, ndofs, nnz = m, m.ndofs, m.ndofs
+
+        def csr_pattern(self, base=0):
+            return np.arange(m.ndofs + 1, dtype=np.int32), np.arange(m.ndofs, dtype=np.int32)
+
+    s = N.LoadStepSolver(_ES(), bc, device="cpu")
+    x = torch.zeros(m.ndofs, dtype=torch.float64)
+    x[3] = 0.4  # not on the equal-step path: the rule still closes the gap in equal parts
+    seen = []
+    for i in range(1, 5):
+        x = s.apply_increment(x, i, 4)
+        seen.append((float(x[3]), float(x[7]), float(x[11])))
+    cur3 = [0.4]
+    for i in range(1, 5):
+        cur3.append(cur3[-1] + (2.0 - cur3[-1]) / (4 - i + 1))
+    assert np.allclose([v[0] for v in seen], cur3[1:], rtol=0, atol=1e-15)
+    assert np.allclose([v[1] for v in seen], [-0.25, -0.5, -0.75, -1.0], rtol=0, atol=1e-15)
+    assert all(v[2] == 0.5 for v in seen)   # fixed (not incremented) values hold from the start
+    assert seen[-1][0] == 2.0
+
+
+def test_config1_uniaxial_exact_solution(oracle):
+    """4x4x4 trilinear cube, Mooney-Rivlin (2, 6), stretch 1.1 in 5 increments:
+    Newton reaches ||r|| <= 1e-10 quadratically at every increment and the
+    converged field is the homogeneous incompressible stretch, with the
+    pressure that makes the lateral faces traction-free."""
+    m = cube_cfg1()
+    lam = 1.1
+    x, reps = oracle_solve(oracle, m, N.uniaxial_symmetry_conditions(m, lam), 5, linear="dense")
+    assert len(reps) == 5 and all(r.converged for r in reps)
+    for r in reps:
+        assert r.iterations <= 5
+        rn = r.residual_norms
+        assert rn[-1] <= 1e-10
+        assert rn[-2] <= 1e-3 * rn[-3] or rn[-2] <= 1e-6   # superlinear tail
+    z = x[:3 * m.nu].numpy().reshape(3, -1)
+    assert np.abs(z[0] - lam * m.X[0]).max() < 1e-11
+    assert np.abs(z[1] - m.X[1] / np.sqrt(lam)).max() < 1e-11
+    assert np.abs(z[2] - m.X[2] / np.sqrt(lam)).max() < 1e-11
+    # sigma = dev(2 c1 B - 2 c2 B^-1) + p I with sigma_yy = 0
+    B = np.array([lam ** 2, 1 / lam, 1 / lam])
+    sb = 2 * 2.0 * B - 2 * 6.0 / B
+    p_exact = -(sb[1] - sb.mean())
+    p = x[3 * m.nu:].numpy()
+    assert np.abs(p - p_exact).max() < 1e-10
+
+
+def test_gmres_matches_dense(oracle):
+    m = quad_small()
+    bc = N.clamped_stretch_shear_conditions(m, 1.15, 0.05)
+    xd, rd = oracle_solve(oracle, m, bc, 2, linear="dense")
+    xg, rg = oracle_solve(oracle, m, bc, 2, linear="gmres", gmres_rtol=1e-8)
+    assert all(r.converged for r in rd + rg)
+    assert [r.iterations for r in rd] == [r.iterations for r in rg]
+    assert float((xd - xg).abs().max()) < 1e-9
+    assert all(max(r.linear_iterations) > 1 for r in rg)
+
+
+def test_line_search_backtracks_on_a_large_step(oracle):
+    """One increment straight to stretch 1.3 / shear 0.1 on the triquadratic
+    mesh: the full Newton step fails the sufficient-decrease test at least
+    once, the cubic backtracking shortens it, and Newton still ends at
+    ||r|| <= 1e-10 with full steps in its quadratic tail."""
+    m = quad_small()
+    x, reps = oracle_solve(oracle, m, N.clamped_stretch_shear_conditions(m, 1.3, 0.1), 1, linear="dense")
+    r = reps[0]
+    assert r.converged
+    assert min(r.line_search_lambdas) < 1.0
+    for f0, f1 in zip(r.residual_norms[:-1], r.residual_norms[1:]):
+        assert f1 < f0   # every accepted step decreases ||r||
+    assert r.line_search_lambdas[-1] == 1.0
+
+
+def test_mixed_split_positions_cover_the_pattern():
+    """Host logic of the mixed path: the uu and coupling positions partition
+    the full pattern (checked on the layout arithmetic alone)."""
+    rp = np.array([0, 5, 9, 13, 15])         # 3 u rows (nu = 1) + 1 p row
+    uu_rp = np.array([0, 4, 7, 10])
+    cp_rp = np.array([0, 1, 2, 3, 5])
+    nu3, nd = 3, 4
+    ku = np.zeros(nd, dtype=np.int64)
+    ku[:nu3] = np.diff(uu_rp)
+    ru = np.repeat(np.arange(nu3), ku[:nu3])
+    uu_pos = rp[ru] + (np.arange(uu_rp[-1]) - uu_rp[ru])
+    rc = np.repeat(np.arange(nd), np.diff(cp_rp))
+    cp_pos = rp[rc] + ku[rc] + (np.arange(cp_rp[-1]) - cp_rp[rc])
+    assert sorted(np.concatenate([uu_pos, cp_pos]).tolist()) == list(range(15))
+
+
+# ------------------------------------------------------------------- GPU
+@pytest.fixture(scope="module")
+def cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from cm_gb300 import _lib
+    _lib.load()
+    return torch.device("cuda")
+
+
+def gpu_solve(m, bc, increments, **opt):
+    from cm_gb300 import FiniteElasticityEquationsSet
+    es = FiniteElasticityEquationsSet(m)
+    s = N.LoadStepSolver(es, bc, N.NewtonOptions(**opt), device="cuda")
+    x, reps = s.solve(torch.from_numpy(N.initial_state(m)).cuda(), increments)
+    return x.cpu(), reps, es
+
+
+@pytest.mark.gpu
+def test_gpu_config1_matches_oracle_newton(cuda, oracle):
+    m = cube_cfg1()
+    bc = N.uniaxial_symmetry_conditions(m, 1.1)
+    xo, ro = oracle_solve(oracle, m, bc, 5, linear="dense")
+    xg, rg, es = gpu_solve(m, bc, 5, linear="dense")
+    assert [r.iterations for r in rg] == [r.iterations for r in ro]
+    for a, b in zip(rg, ro):
+        assert a.converged
+        assert np.allclose(a.residual_norms[:-1], b.residual_norms[:-1], rtol=1e-8)
+    assert float((xg - xo).abs().max()) < 1e-11
+    assert es.launch_count() > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("hp", ["fp64", "double_float"])
+def test_gpu_mixed_jacobian_converges_to_fp64_solution(cuda, oracle, hp):
+    """FP32 Jacobian (BF16x3 tensor cores on the displacement blocks), FP64 or
+    double-float residual: the converged solution meets the same
+    ||r||_2 <= 1e-10 and agrees with the FP64 oracle run."""
+    m = quad_small()
+    bc = N.clamped_stretch_shear_conditions(m, 1.2, 0.1)
+    xo, ro = oracle_solve(oracle, m, bc, 3, linear="dense")
+    xm, rm, _ = gpu_solve(m, bc, 3, linear="dense", precision="mixed", high_precision=hp)
+    assert all(r.converged for r in rm)
+    assert all(r.residual_norms[-1] <= 1e-10 for r in rm)
+    for a, b in zip(rm, ro):
+        assert a.iterations <= b.iterations + 2
+    assert float((xm - xo).abs().max()) < 1e-9
+
+
+@pytest.mark.gpu
+def test_gpu_gmres_path(cuda, oracle):
+    m = quad_small()
+    bc = N.clamped_stretch_shear_conditions(m, 1.15, 0.05)
+    xo, ro = oracle_solve(oracle, m, bc, 2, linear="dense")
+    xg, rg, _ = gpu_solve(m, bc, 2, linear="gmres", gmres_rtol=1e-8)
+    assert all(r.converged for r in rg)
+    assert float((xg - xo).abs().max()) < 1e-9
