@@ -84,11 +84,12 @@ class ClockSampler:
         self.index = index
         self.lines = []
         self.proc = None
+        self.window = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -98,7 +99,17 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def wait_first_sample(self, limit_s=5.0):
+        """Blocks until nvidia-smi has printed its first line (it takes a
+        moment to start), so the timed region is covered by samples."""
+        t0 = time.perf_counter()
+        while self.proc and not self.lines and time.perf_counter() - t0 < limit_s:
+            time.sleep(0.02)
+
+    def mark(self, t0, t1):
+        self.window = (t0, t1)
 
     def __exit__(self, *a):
         if self.proc:
@@ -111,7 +122,13 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if self.window:
+            inside = [ln for t, ln in lines if self.window[0] <= t <= self.window[1] + 0.1]
+            lines = inside if inside else [ln for _, ln in lines[-1:]]
+        else:
+            lines = [ln for _, ln in lines]
+        for ln in lines:
             f = [t.strip() for t in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -237,11 +254,14 @@ def our_arm(args):
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     with ClockSampler(local) as clk:
+        clk.wait_first_sample()
+        w0 = time.perf_counter()
         start.record(stream)
         for _ in range(args.steps):
             step()
         end.record(stream)
         end.synchronize()
+        clk.mark(w0, time.perf_counter())
     launches = es.launch_count() - l0
     es.check_status(xd)
     t = start.elapsed_time(end) / 1e3
@@ -369,7 +389,7 @@ def peaks():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg2", choices=["cfg2", "cfg4", "cfg1"])

@@ -63,10 +63,33 @@ SIGNATURES = {
     "fe_element_jacobians": [_vp, _vp, _i32, _i32, _vp, _vp],
     "fe_set_high_precision": [_vp, _i32],
     "fe_set_surface_pressure": [_vp, _vp],
+    "fe_set_materials": [_vp, _vp],
     "fe_check": [_vp, _vp],
     "fe_launch_count": [_vp, C.POINTER(_i64)],
     "fe_last_error": [C.c_char_p, _i32],
+    "fe_batch_create": [_vp, _i32, C.POINTER(_vp)],
+    "fe_batch_destroy": [_vp],
+    "fe_batch_jacobian_evaluate_mixed": [_vp, _vp, _vp, _vp, _vp, _vp],
+    "fe_batch_check": [_vp, _vp],
+    "fe_batch_set_config": [_vp, _i32, _i32, _i32],
+    "fe_batch_get_config": [_vp, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32), C.POINTER(C.c_double)],
+    "fe_batch_autotune": [_vp, _vp, _vp, _vp, _vp, _i32, _vp],
+    "fe_batch_capture": [_vp, _vp, _vp, _vp, _vp, _vp],
+    "fe_batch_replay": [_vp, _vp],
+    "fe_batch_launch_count": [_vp, C.POINTER(_i64)],
+    # include/cm_warmstart.h
+    "ws_gemm_f32": [_i32, _i32, _i32, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, C.c_float, _vp],
+    "ws_bias_act": [_vp, _vp, _i32, _i32, _i32, _vp],
+    "ws_act_backward": [_vp, _vp, _vp, _i64, _i32, _vp],
+    "ws_column_sum": [_vp, _vp, _i32, _i32, _vp],
+    "ws_mse": [_vp, _vp, _vp, _vp, _i64, _vp],
+    "ws_adam": [_vp, _vp, _vp, _vp, _i64, C.c_float, C.c_float, C.c_float, C.c_float, _i32, _vp],
+    "ws_to_bf16": [_vp, _vp, _i64, _vp],
+    "ws_mlp_forward_bf16": [_i32, _i32, _vp, _vp, _vp, _vp, _vp, _i32, _vp],
 }
+
+WS_ACT_IDENTITY = 0
+WS_ACT_TANH = 1
 
 _lib = None
 

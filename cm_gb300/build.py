@@ -1,6 +1,6 @@
 """In-tree build of libcm_fe.so for sm_103a with plain nvcc.
 
-The two translation units are compiled in parallel and linked into
+The translation units are compiled in parallel and linked into
 ``cm_gb300/_build/libcm_fe.so``.  Host code is compiled without floating-point
 contraction so that the host set-up gives the same bits on x86-64 and aarch64.
 """
@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcm_fe.so")
-SOURCES = ["fe_kernels.cu", "fe_mixed.cu", "fe_surface.cu", "fe_setup.cpp"]
+SOURCES = ["fe_batch.cu", "fe_kernels.cu", "fe_mixed.cu", "fe_surface.cu", "fe_mlp.cu", "fe_setup.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -29,7 +29,7 @@ def _nvcc() -> str:
 
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    files.append(os.path.join(HERE, "..", "include", "cm_fe.h"))
+    files += [os.path.join(HERE, "..", "include", h) for h in ("cm_fe.h", "cm_warmstart.h")]
     return files
 
 

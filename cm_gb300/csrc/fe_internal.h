@@ -86,6 +86,7 @@ struct KParams {
   float* vals_uu;    // FP32 uu values (mixed)
   double* elem_out;  // element-level output
   int res_only;      // mixed kernel: residual only (no Jacobian blocks)
+  int wave;          // mixed kernel: CTAs per launch wave (the SM count)
   int nr, pmode;     // local row nodes per element, pressure interpolation
   const double* surf_p;  // surface pressure values [3][nu] (surface kernel)
   unsigned* status;
@@ -104,5 +105,37 @@ int launch_surface(const HostSetup& s, const KParams& kp, const int32_t* belems,
 
 // Builds the set-up; returns FE_NO_ERROR or a FE_ERR_* code with msg filled.
 int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg);
+
+// Batched mixed assembly (fe_batch.cu): per-member output pointers and the
+// arguments of the persistent launch.
+struct BatchPtrs {
+  const double* x;
+  double* r;
+  double* vals;
+  float* vals_uu;
+};
+
+struct BatchArgs {
+  const KParams* kps;        // [member][colour]
+  const BatchPtrs* ptrs;     // [member]
+  const int32_t* items;      // 4 ints per work item: kp index, first group, groups, element type
+  const int32_t* item_ptr;   // [colour + 1]
+  int ncolours;
+  int ncol_kp;               // colours per member in kps
+  unsigned* bar_count;       // grid barrier state (zero before a launch)
+  unsigned* bar_gen;
+  unsigned* status;          // bit 1: a grid barrier gave up waiting
+  int wave;
+};
+
+// Number of launch variants, their elements per group (triquadratic,
+// trilinear) and dynamic shared memory; the launch returns a cudaError_t.
+int batch_variants();
+int batch_variant_eg(int v, int* egq, int* egl);
+int batch_smem(int v);
+int launch_mixed_batch(int variant, const BatchArgs& a, int ctas_per_sm, int num_sms, void* stream);
+
+// Records the text fe_last_error() returns (per calling thread) and returns code.
+int record_error(int code, const std::string& msg);
 
 }  // namespace cmfe

@@ -487,6 +487,28 @@ struct fe_equations_set {
   std::mutex mu;
 };
 
+struct fe_batch_s {
+  std::vector<fe_handle> members;
+  int device = 0;
+  int num_sms = 0;
+  int ncol = 0;                    // colours per member slot in kps
+  std::vector<KParams> kps;        // [member][colour] (output pointers set per call)
+  KParams* d_kps = nullptr;
+  cmfe::BatchPtrs* d_ptrs = nullptr;
+  cmfe::BatchPtrs* h_ptrs = nullptr;  // pinned copy of the last uploaded table
+  int32_t* d_items = nullptr;
+  int32_t* d_item_ptr = nullptr;
+  unsigned* d_sync = nullptr;      // [0] barrier count, [1] barrier generation, [2] status
+  int variant = 1, ctas_per_sm = 2, block_groups = 1;
+  int items_variant = -1, items_block = -1;
+  int64_t nitems = 0;
+  double tuned_ms = -1.0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int64_t launches = 0;
+  std::mutex mu;
+};
+
 namespace {
 
 template <int N1, int PM, int MODE>
@@ -630,6 +652,105 @@ int finish_status(fe_handle h, cudaStream_t st) {
 }
 
 }  // namespace
+
+namespace {
+
+int member_type(const HostSetup& s) { return (s.n1 == 3 ? 2 : 0) + (s.pmode ? 1 : 0); }
+
+// Work items of every colour for a launch variant: (kp index, first group,
+// groups, element type), element types contiguous within a colour.
+int build_items(fe_batch b, int variant, int block_groups) {
+  if (b->items_variant == variant && b->items_block == block_groups) return FE_NO_ERROR;
+  int egq = 0, egl = 0;
+  if (cmfe::batch_variant_eg(variant, &egq, &egl)) return set_error(FE_ERR_INVALID_ARGUMENT, "unknown batch variant");
+  std::vector<int32_t> items, ptr(1, 0);
+  for (int c = 0; c < b->ncol; ++c) {
+    for (int t = 0; t < 4; ++t)
+      for (size_t m = 0; m < b->members.size(); ++m) {
+        const HostSetup& hs = b->members[m]->hs;
+        if (member_type(hs) != t || c >= hs.ncolours) continue;
+        const int count = hs.colour_ptr[c + 1] - hs.colour_ptr[c];
+        const int eg = hs.n1 == 3 ? egq : egl;
+        const int groups = (count + eg - 1) / eg;
+        for (int g = 0; g < groups; g += block_groups) {
+          items.push_back((int32_t)(m * b->ncol + c));
+          items.push_back(g);
+          items.push_back(std::min(block_groups, groups - g));
+          items.push_back(t);
+        }
+      }
+    ptr.push_back((int32_t)(items.size() / 4));
+  }
+  if (b->d_items) cudaFree(b->d_items);
+  b->d_items = nullptr;
+  if (!items.empty()) CUDA_TRY(cudaMalloc(&b->d_items, items.size() * sizeof(int32_t)));
+  if (!items.empty())
+    CUDA_TRY(cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(b->d_item_ptr, ptr.data(), ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  b->items_variant = variant;
+  b->items_block = block_groups;
+  b->nitems = (int64_t)items.size() / 4;
+  return FE_NO_ERROR;
+}
+
+// Uploads the per-member output pointers when they changed since the last call.
+int batch_set_pointers(fe_batch b, const double* const* x, float* const* uu, double* const* cp, double* const* r,
+                       cudaStream_t st) {
+  const size_t n = b->members.size();
+  bool changed = false;
+  for (size_t m = 0; m < n; ++m) {
+    if (!x[m] || !uu[m] || !cp[m]) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL member pointer");
+    if (!is_device_ptr(x[m]) || !is_device_ptr(uu[m]) || !is_device_ptr(cp[m]) || (r && r[m] && !is_device_ptr(r[m])))
+      return set_error(FE_ERR_INVALID_ARGUMENT, "batched evaluation takes device pointers only");
+    cmfe::BatchPtrs p{x[m], r ? r[m] : nullptr, cp[m], uu[m]};
+    if (std::memcmp(&p, &b->h_ptrs[m], sizeof(p)) != 0) {
+      b->h_ptrs[m] = p;
+      changed = true;
+    }
+  }
+  if (changed) {
+    // the pinned table is rewritten by the next call: wait for this copy
+    CUDA_TRY(cudaMemcpyAsync(b->d_ptrs, b->h_ptrs, n * sizeof(cmfe::BatchPtrs), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  return FE_NO_ERROR;
+}
+
+int batch_launch(fe_batch b, cudaStream_t st) {
+  int rc = build_items(b, b->variant, b->block_groups);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned), st));
+  cmfe::BatchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.kps = b->d_kps;
+  a.ptrs = b->d_ptrs;
+  a.items = b->d_items;
+  a.item_ptr = b->d_item_ptr;
+  a.ncolours = b->ncol;
+  a.ncol_kp = b->ncol;
+  a.bar_count = b->d_sync;
+  a.bar_gen = b->d_sync + 1;
+  a.status = b->d_sync + 2;
+  if (b->nitems == 0) return FE_NO_ERROR;
+  const int e = cmfe::launch_mixed_batch(b->variant, a, b->ctas_per_sm, b->num_sms, st);
+  if (e != 0) return set_error(FE_ERR_CUDA, std::string("batched kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+  b->launches++;
+  return FE_NO_ERROR;
+}
+
+int check_batch(fe_batch b) {
+  if (!b) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL batch");
+  int cur = 0;
+  CUDA_TRY(cudaGetDevice(&cur));
+  if (cur != b->device) return set_error(FE_ERR_INVALID_ARGUMENT, "batch belongs to another CUDA device");
+  return FE_NO_ERROR;
+}
+
+}  // namespace
+
+namespace cmfe {
+int record_error(int code, const std::string& msg) { return set_error(code, msg); }
+}  // namespace cmfe
 
 extern "C" {
 
@@ -928,6 +1049,15 @@ int fe_set_surface_pressure(fe_handle h, const double* values) {
   return FE_NO_ERROR;
 }
 
+int fe_set_materials(fe_handle h, const double* materials) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (!materials) return set_error(FE_ERR_INVALID_ARGUMENT, "materials is NULL");
+  std::lock_guard<std::mutex> lk(h->mu);
+  CUDA_TRY(cudaMemcpy(h->d_mat, materials, sizeof(double) * h->hs.mat.size(), cudaMemcpyDefault));
+  return FE_NO_ERROR;
+}
+
 int fe_set_high_precision(fe_handle h, int32_t mode) {
   if (!h) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL handle");
   if (mode != FE_HIGH_PRECISION_FP64 && mode != FE_HIGH_PRECISION_DOUBLE_FLOAT)
@@ -946,6 +1076,216 @@ int fe_check(fe_handle h, void* stream) {
 int fe_launch_count(fe_handle h, int64_t* count) {
   if (!h || !count) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL argument");
   *count = h->launches;
+  return FE_NO_ERROR;
+}
+
+int fe_batch_create(const fe_handle* handles, int32_t count, fe_batch* out) {
+  if (!out) return set_error(FE_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (!handles || count <= 0) return set_error(FE_ERR_INVALID_ARGUMENT, "empty batch");
+  int cur = 0;
+  CUDA_TRY(cudaGetDevice(&cur));
+  auto b = new (std::nothrow) fe_batch_s;
+  if (!b) return set_error(FE_ERR_OUT_OF_MEMORY, "batch allocation failed");
+  b->device = cur;
+  int rc = FE_NO_ERROR;
+  for (int32_t i = 0; i < count && !rc; ++i) {
+    if (!handles[i]) rc = set_error(FE_ERR_INVALID_ARGUMENT, "NULL member handle");
+    else if (handles[i]->device != cur) rc = set_error(FE_ERR_INVALID_ARGUMENT, "member on another CUDA device");
+    else {
+      b->members.push_back(handles[i]);
+      b->ncol = std::max(b->ncol, handles[i]->hs.ncolours);
+    }
+  }
+  if (!rc) {
+    b->num_sms = b->members[0]->num_sms;
+    b->kps.resize((size_t)count * b->ncol);
+    for (int32_t m = 0; m < count; ++m) {
+      fe_handle h = b->members[m];
+      for (int c = 0; c < b->ncol; ++c) {
+        KParams k = base_params(h);
+        if (c < h->hs.ncolours) {
+          k.elems = h->d_colour_elems + h->hs.colour_ptr[c];
+          k.count = h->hs.colour_ptr[c + 1] - h->hs.colour_ptr[c];
+        }
+        b->kps[(size_t)m * b->ncol + c] = k;
+      }
+    }
+    auto fail = [&](cudaError_t e) {
+      return e == cudaSuccess ? FE_NO_ERROR : set_error(FE_ERR_CUDA, std::string("batch set-up: ") + cudaGetErrorString(e));
+    };
+    rc = fail(cudaMalloc(&b->d_kps, b->kps.size() * sizeof(KParams)));
+    if (!rc) rc = fail(cudaMemcpy(b->d_kps, b->kps.data(), b->kps.size() * sizeof(KParams), cudaMemcpyHostToDevice));
+    if (!rc) rc = fail(cudaMalloc(&b->d_ptrs, (size_t)count * sizeof(cmfe::BatchPtrs)));
+    if (!rc) rc = fail(cudaMallocHost(&b->h_ptrs, (size_t)count * sizeof(cmfe::BatchPtrs)));
+    if (!rc) std::memset(b->h_ptrs, 0, (size_t)count * sizeof(cmfe::BatchPtrs));
+    if (!rc) rc = fail(cudaMalloc(&b->d_item_ptr, (size_t)(b->ncol + 1) * sizeof(int32_t)));
+    if (!rc) rc = fail(cudaMalloc(&b->d_sync, 4 * sizeof(unsigned)));
+    if (!rc) rc = fail(cudaMemset(b->d_sync, 0, 4 * sizeof(unsigned)));
+  }
+  if (rc) {
+    fe_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return FE_NO_ERROR;
+}
+
+int fe_batch_destroy(fe_batch b) {
+  if (!b) return FE_NO_ERROR;
+  if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  void* ptrs[] = {b->d_kps, b->d_ptrs, b->d_items, b->d_item_ptr, b->d_sync};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (b->h_ptrs) cudaFreeHost(b->h_ptrs);
+  delete b;
+  return FE_NO_ERROR;
+}
+
+int fe_batch_jacobian_evaluate_mixed(fe_batch b, const double* const* x, float* const* values_uu,
+                                     double* const* values_coupling, double* const* r, void* stream) {
+  int rc = check_batch(b);
+  if (rc) return rc;
+  if (!x || !values_uu || !values_coupling) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL pointer array");
+  std::lock_guard<std::mutex> lk(b->mu);
+  for (fe_handle h : b->members)
+    if (h->has_surfp) return set_error(FE_ERR_NOT_SUPPORTED, "batched evaluation of a member with surface pressure");
+  cudaStream_t st = (cudaStream_t)stream;
+  if ((rc = batch_set_pointers(b, x, values_uu, values_coupling, r, st))) return rc;
+  return batch_launch(b, st);
+}
+
+int fe_batch_check(fe_batch b, void* stream) {
+  int rc = check_batch(b);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned v = 0;
+  CUDA_TRY(cudaMemcpyAsync(&v, b->d_sync + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemsetAsync(b->d_sync + 2, 0, sizeof(unsigned), st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (v & 2u) return set_error(FE_ERR_CUDA, "batched launch: a grid barrier gave up waiting");
+  for (fe_handle h : b->members)
+    if ((rc = finish_status(h, st))) return rc;
+  return FE_NO_ERROR;
+}
+
+int fe_batch_set_config(fe_batch b, int32_t variant, int32_t ctas_per_sm, int32_t block_groups) {
+  int rc = check_batch(b);
+  if (rc) return rc;
+  if (variant < 0 || variant >= cmfe::batch_variants() || ctas_per_sm < 1 || ctas_per_sm > 4 || block_groups < 1)
+    return set_error(FE_ERR_INVALID_ARGUMENT, "invalid batch configuration");
+  std::lock_guard<std::mutex> lk(b->mu);
+  b->variant = variant;
+  b->ctas_per_sm = ctas_per_sm;
+  b->block_groups = block_groups;
+  return FE_NO_ERROR;
+}
+
+int fe_batch_get_config(fe_batch b, int32_t* variant, int32_t* ctas_per_sm, int32_t* block_groups, double* tuned_ms) {
+  int rc = check_batch(b);
+  if (rc) return rc;
+  if (variant) *variant = b->variant;
+  if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm;
+  if (block_groups) *block_groups = b->block_groups;
+  if (tuned_ms) *tuned_ms = b->tuned_ms;
+  return FE_NO_ERROR;
+}
+
+int fe_batch_autotune(fe_batch b, const double* const* x, float* const* values_uu, double* const* values_coupling,
+                      double* const* r, int32_t repeats, void* stream) {
+  int rc = check_batch(b);
+  if (rc) return rc;
+  if (!x || !values_uu || !values_coupling || repeats < 1) return set_error(FE_ERR_INVALID_ARGUMENT, "bad arguments");
+  std::lock_guard<std::mutex> lk(b->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  if ((rc = batch_set_pointers(b, x, values_uu, values_coupling, r, st))) return rc;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  const int keep_v = b->variant, keep_c = b->ctas_per_sm, keep_b = b->block_groups;
+  double best = 1e300;
+  int bv = keep_v, bc = keep_c, bb = keep_b;
+  const int blocks[] = {1, 2, 4};
+  for (int v = 0; v < cmfe::batch_variants() && !rc; ++v)
+    for (int cps = 1; cps <= 2 && !rc; ++cps) {
+      // skip a CTA count the shared memory cannot hold (the launch would use fewer)
+      if (cps * (cmfe::batch_smem(v) + 1024) > 232448) continue;
+      for (int bg : blocks) {
+        b->variant = v;
+        b->ctas_per_sm = cps;
+        b->block_groups = bg;
+        if ((rc = batch_launch(b, st))) break;  // warm-up (and table upload)
+        cudaEventRecord(e0, st);
+        for (int i = 0; i < repeats && !rc; ++i) rc = batch_launch(b, st);
+        cudaEventRecord(e1, st);
+        if (rc) break;
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double per = ms / repeats;
+        if (per < best) {
+          best = per;
+          bv = v;
+          bc = cps;
+          bb = bg;
+        }
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) {
+    b->variant = keep_v;
+    b->ctas_per_sm = keep_c;
+    b->block_groups = keep_b;
+    return rc;
+  }
+  b->variant = bv;
+  b->ctas_per_sm = bc;
+  b->block_groups = bb;
+  b->tuned_ms = best;
+  return build_items(b, bv, bb);
+}
+
+int fe_batch_capture(fe_batch b, const double* const* x, float* const* values_uu, double* const* values_coupling,
+                     double* const* r, void* stream) {
+  int rc = check_batch(b);
+  if (rc) return rc;
+  if (!x || !values_uu || !values_coupling) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL pointer array");
+  std::lock_guard<std::mutex> lk(b->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  if ((rc = batch_set_pointers(b, x, values_uu, values_coupling, r, st))) return rc;
+  if ((rc = build_items(b, b->variant, b->block_groups))) return rc;
+  cudaStream_t cs;
+  CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->graph_exec = nullptr;
+  b->graph = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    rc = batch_launch(b, cs);
+    e = cudaStreamEndCapture(cs, &b->graph);
+    if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&b->graph_exec, b->graph, 0);
+  }
+  cudaStreamDestroy(cs);
+  if (rc) return rc;
+  if (e != cudaSuccess) return set_error(FE_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
+  return FE_NO_ERROR;
+}
+
+int fe_batch_replay(fe_batch b, void* stream) {
+  int rc = check_batch(b);
+  if (rc) return rc;
+  if (!b->graph_exec) return set_error(FE_ERR_INVALID_ARGUMENT, "no captured graph: call fe_batch_capture first");
+  CUDA_TRY(cudaGraphLaunch(b->graph_exec, (cudaStream_t)stream));
+  b->launches++;
+  return FE_NO_ERROR;
+}
+
+int fe_batch_launch_count(fe_batch b, int64_t* count) {
+  if (!b || !count) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL argument");
+  *count = b->launches;
   return FE_NO_ERROR;
 }
 

@@ -172,6 +172,14 @@ class FiniteElasticityEquationsSet:
             values = np.ascontiguousarray(values, dtype=np.float64)
         check(_lib.load().fe_set_surface_pressure(self._h, _ptr(values)))
 
+    def set_materials(self, materials):
+        """New material parameters, same layout as the mesh's (host array)."""
+        mats = np.ascontiguousarray(materials, dtype=np.float64)
+        if mats.shape != np.shape(self.mesh.materials):
+            raise ValueError("materials must have shape %s" % (np.shape(self.mesh.materials),))
+        check(_lib.load().fe_set_materials(self._h, mats.ctypes.data))
+        self.materials = mats
+
     def set_high_precision(self, mode: str):
         """'fp64' (IEEE binary64, default) or 'double_float' (FP32 pairs, about
         48 significant bits) for the residual and pressure-coupling parts of

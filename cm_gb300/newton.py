@@ -39,11 +39,12 @@ class NewtonOptions:
     min_lambda: float = 1e-10
     precision: str = "fp64"      # "fp64" Jacobian, or "mixed" (FP32 displacement block)
     high_precision: str = "fp64"  # residual/coupling arithmetic of the mixed path
-    linear: str = "auto"         # "dense", "gmres" or "auto" (dense up to dense_limit free dofs)
+    linear: str = "auto"         # "dense", "gmres" (block-Jacobi), "mg" (multigrid block preconditioner)
+    #                              or "auto" (dense up to dense_limit free dofs)
     dense_limit: int = 12000
     gmres_rtol: float = 1e-6
     gmres_restart: int = 80
-    gmres_max_iterations: int = 3000
+    gmres_max_iterations: int = 600
 
 
 @dataclass
@@ -105,10 +106,29 @@ class FreeDofSystem:
         self.is_p = torch.from_numpy(np.nonzero(free_mask)[0] >= 3 * es.mesh.nu).to(device)
         self.is_diag = (self.row == self.col)
         self.device = device
+        # displacement block A (free u x free u) and coupling block B (p x free u):
+        # free u dofs come first, and in every row the u columns precede the p columns
+        nfu = int((np.nonzero(free_mask)[0] < 3 * es.mesh.nu).sum())
+        self.nfu, self.nfp = nfu, self.nf - nfu
+        am = (r < nfu) & (c < nfu)
+        bm = (r >= nfu) & (c < nfu)
+        self.a_sel = torch.from_numpy(np.nonzero(am)[0]).to(device)
+        self.a_crow = torch.from_numpy(np.concatenate([[0], np.cumsum(np.bincount(r[am], minlength=nfu))])).to(device)
+        self.a_col = torch.from_numpy(c[am].astype(np.int64)).to(device)
+        self.b_sel = torch.from_numpy(np.nonzero(bm)[0]).to(device)
+        self.b_crow = torch.from_numpy(
+            np.concatenate([[0], np.cumsum(np.bincount(r[bm] - nfu, minlength=self.nfp))])).to(device)
+        self.b_col = torch.from_numpy(c[bm].astype(np.int64)).to(device)
 
     def matrix(self, vals_full):
         v = vals_full[self.sel]
         return torch.sparse_csr_tensor(self.crow, self.col, v, size=(self.nf, self.nf))
+
+    def blocks(self, J, dtype_a=torch.float64):
+        v = J.values()
+        A = torch.sparse_csr_tensor(self.a_crow, self.a_col, v[self.a_sel].to(dtype_a), size=(self.nfu, self.nfu))
+        B = torch.sparse_csr_tensor(self.b_crow, self.b_col, v[self.b_sel], size=(self.nfp, self.nfu))
+        return A, B
 
 
 def _gmres(A, b, M, rtol, restart, max_it):
@@ -195,12 +215,28 @@ class LoadStepSolver:
             self.cp_pos = torch.from_numpy(cp_pos).to(self.device)
             self.vu = torch.empty(es.nnz_uu, dtype=torch.float32, device=self.device)
             self.vc = torch.empty(es.nnz_coupling, dtype=torch.float64, device=self.device)
+        if self.opt.linear == "mg":
+            from .multigrid import BoxMultigrid, MassSolver, pressure_mass_matrix
+            m = es.mesh
+            self.mg = BoxMultigrid(m.grid_u, m.nxi_u, self.free_mask[:3 * m.nu], self.device,
+                                   torch.float32 if self.opt.precision == "mixed" else torch.float64)
+            fp = self.free_mask[3 * m.nu:]
+            Mp = pressure_mass_matrix(m)[fp][:, fp]
+            self.mass_p = torch.from_numpy(Mp.diagonal().copy()).to(self.device)
+            self.mass_solver = MassSolver(Mp, self.device)
         self.vals = torch.empty(es.nnz, dtype=torch.float64, device=self.device)
         self.r = torch.empty(es.ndofs, dtype=torch.float64, device=self.device)
 
     def _sync(self):
         if self.device.type == "cuda":
             torch.cuda.synchronize(self.device)
+
+    def update_conditions(self, bc: DirichletConditions):
+        """New Dirichlet values on the same set of dofs (the free-dof system,
+        its index maps and the multigrid hierarchy are kept)."""
+        if not np.array_equal(bc.dofs, self.bc.dofs):
+            raise ValueError("the Dirichlet dof set must not change")
+        self.bc = bc
 
     # -------------------------------------------------------------- pieces
     def apply_increment(self, x, i, n):
@@ -243,10 +279,34 @@ class LoadStepSolver:
         inv[p] = -1.0 / torch.where(sd[p] != 0, sd[p], torch.ones_like(sd[p]))
         return lambda w: inv * w
 
+    def _mg_preconditioner(self, J):
+        """Block lower-triangular preconditioner [A 0; B -S]^-1 with a multigrid
+        V-cycle for A and the scaled lumped pressure mass for S."""
+        S = self.sys
+        mg_dtype = torch.float32 if self.opt.precision == "mixed" else torch.float64
+        A, B = S.blocks(J, mg_dtype)
+        self.mg.setup(A)
+        dA = self.mg.dinv[0].to(torch.float64)
+        sd = torch.zeros(S.nfp, dtype=torch.float64, device=self.device)
+        bv = B.values()
+        brow = torch.repeat_interleave(torch.arange(S.nfp, device=self.device), B.crow_indices()[1:] - B.crow_indices()[:-1])
+        sd.index_add_(0, brow, bv * bv * dA[B.col_indices()])
+        scale = float(torch.median(sd / self.mass_p))
+        nfu = S.nfu
+
+        def apply(w):
+            zu = self.mg.vcycle(w[:nfu].to(mg_dtype)).to(torch.float64)
+            zp = self.mass_solver.solve(B @ zu - w[nfu:]) / scale
+            return torch.cat([zu, zp])
+        return apply
+
     def linear_solve(self, A, b):
         if self.opt.linear == "dense" or (self.opt.linear == "auto" and self.sys.nf <= self.opt.dense_limit):
             D = A.to_dense()
             return torch.linalg.solve(D, b), 1
+        if self.opt.linear == "mg":
+            M = self._mg_preconditioner(A)
+            return _gmres(A, b, M, self.opt.gmres_rtol, self.opt.gmres_restart, self.opt.gmres_max_iterations)
         M = self._preconditioner(A)
         return _gmres(A, b, M, self.opt.gmres_rtol, self.opt.gmres_restart, self.opt.gmres_max_iterations)
 

@@ -145,6 +145,14 @@ int fe_mixed_layout(fe_handle h, int64_t* nnz_uu, int64_t* nnz_coupling, int32_t
  * every later residual and Jacobian evaluation. */
 int fe_set_surface_pressure(fe_handle h, const double* values);
 
+/* Replaces the material parameters given to fe_create (same layout: one set
+ * of num_material_components values, or one per element when
+ * materials_per_element was set), as an update of the reference's materials
+ * field parameter set does for every later evaluation
+ * (finite_elasticity_routines.f90:652 reads them per Gauss point).  Host or
+ * device memory; copied. */
+int fe_set_materials(fe_handle h, const double* materials);
+
 /* Arithmetic of the high-precision parts of fe_residual_evaluate and
  * fe_jacobian_evaluate_mixed (the residual and the displacement-pressure
  * coupling blocks).  FE_HIGH_PRECISION_FP64 (the default) uses IEEE binary64.
@@ -164,6 +172,46 @@ int fe_set_high_precision(fe_handle h, int32_t mode);
 int fe_element_size(fe_handle h, int32_t* n);
 int fe_element_residuals(fe_handle h, const double* x, int32_t first, int32_t count, double* out, void* stream);
 int fe_element_jacobians(fe_handle h, const double* x, int32_t first, int32_t count, double* out, void* stream);
+
+/* ---- Batched assembly (no counterpart in the reference, which evaluates one
+ * equations set per call).  A batch groups independent equations sets of the
+ * current device (any mix of trilinear / triquadratic elements and pressure
+ * interpolations) and assembles all of them with the mixed-precision kernel in
+ * ONE persistent cooperative launch that walks the element colours in order,
+ * with a grid barrier between colours.  The result is bit-identical to one
+ * fe_jacobian_evaluate_mixed call per member.  The member handles must outlive
+ * the batch; members with surface pressure are not supported. */
+typedef struct fe_batch_s* fe_batch;
+
+int fe_batch_create(const fe_handle* handles, int32_t count, fe_batch* out);
+int fe_batch_destroy(fe_batch b);
+
+/* x[i], values_uu[i], values_coupling[i] (and r[i] when r is not NULL) are
+ * DEVICE pointers of member i, in the layouts of fe_jacobian_evaluate_mixed;
+ * the arrays of pointers are host arrays of length count.  Asynchronous on
+ * stream; fe_batch_check() reports numerical and launch failures. */
+int fe_batch_jacobian_evaluate_mixed(fe_batch b, const double* const* x, float* const* values_uu,
+                                     double* const* values_coupling, double* const* r, void* stream);
+int fe_batch_check(fe_batch b, void* stream);
+
+/* Launch configuration: variant (elements per group for triquadratic /
+ * trilinear members: 0 = 4/8, 1 = 4/4, 2 = 2/4, 3 = 2/2), CTAs per SM, and
+ * element groups per work item (the colour-block size). */
+int fe_batch_set_config(fe_batch b, int32_t variant, int32_t ctas_per_sm, int32_t block_groups);
+int fe_batch_get_config(fe_batch b, int32_t* variant, int32_t* ctas_per_sm, int32_t* block_groups,
+                        double* tuned_ms);
+
+/* Autotuner: times every launch configuration (repeats launches each, CUDA
+ * events on stream) on the given buffers and keeps the fastest.  Synchronous. */
+int fe_batch_autotune(fe_batch b, const double* const* x, float* const* values_uu,
+                      double* const* values_coupling, double* const* r, int32_t repeats, void* stream);
+
+/* Captures one batched assembly with the given buffers into a CUDA graph;
+ * fe_batch_replay() launches it on stream (same buffers, current inputs). */
+int fe_batch_capture(fe_batch b, const double* const* x, float* const* values_uu,
+                     double* const* values_coupling, double* const* r, void* stream);
+int fe_batch_replay(fe_batch b, void* stream);
+int fe_batch_launch_count(fe_batch b, int64_t* count);
 
 /* Waits for the handle's work on `stream` and reports numerical problems
  * seen by the kernels since the last call (FE_ERR_NUMERICAL) — the device

@@ -199,6 +199,15 @@ class EquationsSet:
     def set_surface_pressure(self, values):
         self.prob.set_surface_pressure(None if values is None else np.asarray(values))
 
+    def set_materials(self, materials):
+        import copy
+        m = copy.copy(self.mesh)
+        m.materials = np.asarray(materials, dtype=np.float64)
+        sp = self.prob.surf_p
+        self.prob = Problem(m)
+        if sp is not None:
+            self.prob.set_surface_pressure(sp)
+
     def residual_evaluate(self, x, r):
         _, res = self.prob.assemble(np.asarray(x), self.rp1, self.col1, jacobian=False, residual=True,
                                     nthreads=self.nthreads)
