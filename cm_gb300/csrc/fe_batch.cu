@@ -8,8 +8,9 @@
 // so a CTA reloads its constant tables rarely), then all CTAs meet at a grid
 // barrier before colour c + 1.  Within a member the colour order is the one
 // of the single-set path, so every CSR slot receives its contributions in the
-// same order and the result is bit-identical to one fe_jacobian_evaluate_mixed
-// call per member.
+// same order: repeated launches are bit-identical, and the result agrees with
+// one fe_jacobian_evaluate_mixed call per member to the rounding of the
+// separately compiled device code.
 //
 // The grid barrier spins with a bounded number of polls: if it ever gives up
 // (which only a non-co-resident grid could cause, and the cooperative launch

@@ -42,7 +42,7 @@ def _ptr(a):
 
 
 def _stream(a):
-    if isinstance(a, np.ndarray) or a is None:
+    if isinstance(a, np.ndarray) or a is None or not getattr(a, "is_cuda", False):
         return None
     import torch
     return C.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
@@ -215,3 +215,75 @@ class FiniteElasticityEquationsSet:
             else:
                 out[a:b] = vc[cp_rp[r]:cp_rp[r + 1]]
         return out
+
+
+class EquationsSetBatch:
+    """Many independent equations sets assembled in one persistent launch
+    (fe_batch_* of include/cm_fe.h).  Buffers are CUDA tensors."""
+
+    def __init__(self, sets):
+        self.sets = list(sets)
+        arr = (C.c_void_p * len(self.sets))(*[s.handle for s in self.sets])
+        b = C.c_void_p()
+        check(_lib.load().fe_batch_create(arr, len(self.sets), C.byref(b)))
+        self._b = b
+
+    def close(self):
+        if getattr(self, "_b", None):
+            _lib.load().fe_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _arrays(self, xs, vus, vcs, rs):
+        n = len(self.sets)
+        if not (len(xs) == len(vus) == len(vcs) == n) or (rs is not None and len(rs) != n):
+            raise ValueError("one buffer per member is required")
+        P = C.c_void_p * n
+        a = [P(*[t.data_ptr() for t in lst]) for lst in (xs, vus, vcs)]
+        r = P(*[t.data_ptr() for t in rs]) if rs is not None else None
+        return a[0], a[1], a[2], r
+
+    def allocate(self, device):
+        """Output buffers (values_uu, values_coupling, r) for every member."""
+        import torch
+        vus = [torch.empty(s.nnz_uu, dtype=torch.float32, device=device) for s in self.sets]
+        vcs = [torch.empty(s.nnz_coupling, dtype=torch.float64, device=device) for s in self.sets]
+        rs = [torch.empty(s.ndofs, dtype=torch.float64, device=device) for s in self.sets]
+        return vus, vcs, rs
+
+    def jacobian_evaluate_mixed(self, xs, vus, vcs, rs=None):
+        x, u, c, r = self._arrays(xs, vus, vcs, rs)
+        check(_lib.load().fe_batch_jacobian_evaluate_mixed(self._b, x, u, c, r, _stream(xs[0])))
+
+    def check(self, like=None):
+        check(_lib.load().fe_batch_check(self._b, _stream(like)))
+
+    def set_config(self, variant, ctas_per_sm, block_groups):
+        check(_lib.load().fe_batch_set_config(self._b, variant, ctas_per_sm, block_groups))
+
+    def config(self):
+        v, c, g, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_double()
+        check(_lib.load().fe_batch_get_config(self._b, C.byref(v), C.byref(c), C.byref(g), C.byref(ms)))
+        return {"variant": v.value, "ctas_per_sm": c.value, "block_groups": g.value, "tuned_ms": ms.value}
+
+    def autotune(self, xs, vus, vcs, rs=None, repeats=3):
+        x, u, c, r = self._arrays(xs, vus, vcs, rs)
+        check(_lib.load().fe_batch_autotune(self._b, x, u, c, r, repeats, _stream(xs[0])))
+        return self.config()
+
+    def capture(self, xs, vus, vcs, rs=None):
+        x, u, c, r = self._arrays(xs, vus, vcs, rs)
+        check(_lib.load().fe_batch_capture(self._b, x, u, c, r, _stream(xs[0])))
+
+    def replay(self, like):
+        check(_lib.load().fe_batch_replay(self._b, _stream(like)))
+
+    def launch_count(self):
+        n = C.c_int64()
+        check(_lib.load().fe_batch_launch_count(self._b, C.byref(n)))
+        return n.value

@@ -140,3 +140,25 @@ def deformed_state(mesh: Mesh, stretch=1.1, shear=0.05, noise=0.0, pressure=-1.0
         z += rng.uniform(-noise * hmin, noise * hmin, size=z.shape)
     p = pressure * (1.0 + 0.1 * rng.uniform(-1.0, 1.0, size=mesh.n_pressure))
     return np.concatenate([z.ravel(), p])
+
+
+def batch_meshes(n=256, seed=0, edge_range=(4, 24), length_range=(0.5, 2.0), c_range=(0.5, 10.0),
+                 stretch_range=(1.0, 1.3)):
+    """Seeded batch of independent box problems: per-edge element counts
+    uniform in edge_range, edge lengths uniform in length_range, trilinear
+    (element-constant pressure) or triquadratic (trilinear nodal pressure)
+    elements with probability 1/2 each, Mooney-Rivlin c1, c2 log-uniform in
+    c_range, and a uniaxial stretch uniform in stretch_range.  Returns
+    (meshes, stretches)."""
+    rng = np.random.default_rng(seed)
+    meshes, stretches = [], []
+    lc = np.log(c_range)
+    for _ in range(n):
+        dims = tuple(int(v) for v in rng.integers(edge_range[0], edge_range[1] + 1, size=3))
+        lengths = tuple(float(v) for v in rng.uniform(*length_range, size=3))
+        quad = bool(rng.integers(0, 2))
+        c = np.exp(rng.uniform(*lc, size=2))
+        meshes.append(regular_box(*dims, lengths=lengths, nxi_u=3 if quad else 2,
+                                  pressure="node" if quad else "element", law=MR, materials=tuple(c)))
+        stretches.append(float(rng.uniform(*stretch_range)))
+    return meshes, stretches

@@ -178,9 +178,11 @@ int fe_element_jacobians(fe_handle h, const double* x, int32_t first, int32_t co
  * current device (any mix of trilinear / triquadratic elements and pressure
  * interpolations) and assembles all of them with the mixed-precision kernel in
  * ONE persistent cooperative launch that walks the element colours in order,
- * with a grid barrier between colours.  The result is bit-identical to one
- * fe_jacobian_evaluate_mixed call per member.  The member handles must outlive
- * the batch; members with surface pressure are not supported. */
+ * with a grid barrier between colours.  Repeated launches are bit-identical;
+ * the result agrees with one fe_jacobian_evaluate_mixed call per member to
+ * FP32 rounding in the displacement block and FP64 rounding elsewhere.  The
+ * member handles must outlive the batch; members with surface pressure are
+ * not supported; the residual and coupling blocks are computed in FP64. */
 typedef struct fe_batch_s* fe_batch;
 
 int fe_batch_create(const fe_handle* handles, int32_t count, fe_batch* out);

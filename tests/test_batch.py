@@ -1,0 +1,110 @@
+"""Batched assembly: many equations sets in one persistent launch.
+
+Every launch configuration the autotuner can choose, and the captured CUDA
+graph, must agree with one single-set mixed evaluation per member: the FP64
+residual and coupling blocks to 1e-12 of the array's largest entry, the FP32
+displacement block to 1e-5 of its largest entry (the batched kernel is a
+separate compilation of the same device code, so the compiler may fuse a
+few multiply-adds differently).  Repeated launches of one configuration must
+be bit-identical (colour order fixes the order of every CSR slot's sum).
+"""
+import numpy as np
+import pytest
+
+from cm_gb300 import mesh as M
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as _torch
+    if not _torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from cm_gb300 import _lib
+    _lib.load()
+    return _torch
+
+
+def members():
+    out = [
+        M.regular_box(3, 2, 2, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0), perturb=0.1, seed=1),
+        M.regular_box(4, 3, 2, nxi_u=2, pressure="element", law=M.MR, materials=(1.0, 3.0), perturb=0.1, seed=2),
+        M.regular_box(2, 2, 3, nxi_u=3, pressure="element", law=M.MR, materials=(0.7, 5.0)),
+        M.regular_box(3, 3, 3, nxi_u=2, pressure="node", law=M.MR, materials=(4.0, 1.0), perturb=0.05, seed=3),
+        M.regular_box(2, 3, 2, lengths=(2.0, 1.0, 0.5), nxi_u=3, pressure="node", law=M.GUCCIONE,
+                      materials=(0.88, 18.5, 3.58, 1.63), fibre=np.array([[0.3], [0.1], [-0.2]])),
+    ]
+    meshes, _ = M.batch_meshes(6, seed=5, edge_range=(1, 5))
+    return out + meshes
+
+
+def _setup(torch):
+    from cm_gb300 import EquationsSetBatch, FiniteElasticityEquationsSet
+    ms = members()
+    sets = [FiniteElasticityEquationsSet(m) for m in ms]
+    xs = [torch.from_numpy(M.deformed_state(m, stretch=1.05 + 0.01 * i, shear=0.03, noise=0.02, seed=i)).cuda()
+          for i, m in enumerate(ms)]
+    refs = []
+    for s, x in zip(sets, xs):
+        r = torch.empty_like(x)
+        vu, vc = s.jacobian_evaluate_mixed(x, r=r)
+        s.check_status(x)
+        refs.append((vu.clone(), vc.clone(), r.clone()))
+    return sets, xs, refs, EquationsSetBatch(sets)
+
+
+def _close(torch, refs, vus, vcs, rs):
+    for i, ((a, b, c), u, v, w) in enumerate(zip(refs, vus, vcs, rs)):
+        for ref, got, tol in ((a, u, 1e-5), (b, v, 1e-12), (c, w, 1e-12)):
+            assert not torch.isnan(got).any(), "member %d: entries not written" % i
+            err = float((got.double() - ref.double()).abs().max())
+            assert err <= tol * float(ref.double().abs().max()), "member %d: %.3e" % (i, err)
+
+
+def test_batch_matches_single_set_bitwise(torch):
+    sets, xs, refs, batch = _setup(torch)
+    vus, vcs, rs = batch.allocate("cuda")
+    for variant in range(4):
+        for cps in (1, 2):
+            for bg in (1, 3):
+                batch.set_config(variant, cps, bg)
+                for t in vus + vcs + rs:
+                    t.fill_(float("nan"))
+                batch.jacobian_evaluate_mixed(xs, vus, vcs, rs)
+                batch.check(xs[0])
+                _close(torch, refs, vus, vcs, rs)
+                first = [t.clone() for t in vus + vcs + rs]
+                batch.jacobian_evaluate_mixed(xs, vus, vcs, rs)
+                batch.check(xs[0])
+                assert all(torch.equal(a, b) for a, b in zip(first, vus + vcs + rs))
+    assert batch.launch_count() == 32
+
+
+def test_autotune_and_graph_replay(torch):
+    sets, xs, refs, batch = _setup(torch)
+    vus, vcs, rs = batch.allocate("cuda")
+    cfg = batch.autotune(xs, vus, vcs, rs, repeats=2)
+    assert 0 <= cfg["variant"] < 4 and cfg["tuned_ms"] > 0
+    batch.capture(xs, vus, vcs, rs)
+    for t in vus + vcs + rs:
+        t.zero_()
+    batch.replay(xs[0])
+    batch.check(xs[0])
+    _close(torch, refs, vus, vcs, rs)
+    # new inputs in the same buffers: the replay sees them
+    xs[0].mul_(1.01)
+    r = torch.empty_like(xs[0])
+    vu0, vc0 = sets[0].jacobian_evaluate_mixed(xs[0], r=r)
+    batch.replay(xs[0])
+    batch.check(xs[0])
+    _close(torch, [(vu0, vc0, r)], vus[:1], vcs[:1], rs[:1])
+
+
+def test_batch_rejects_host_pointers(torch):
+    from cm_gb300 import FEError
+    sets, xs, refs, batch = _setup(torch)
+    vus, vcs, rs = batch.allocate("cuda")
+    xs_host = [x.cpu() for x in xs]
+    with pytest.raises(FEError):
+        batch.jacobian_evaluate_mixed(xs_host, vus, vcs, rs)
