@@ -28,6 +28,7 @@ FE_HIGH_PRECISION_FP64 = 0
 FE_HIGH_PRECISION_DOUBLE_FLOAT = 1
 FE_PRESSURE_ELEMENT_BASED = 0
 FE_PRESSURE_NODE_BASED = 1
+FE_NOALLOC_MAX_DOFS = 1048576
 
 
 class FEError(RuntimeError):
@@ -55,6 +56,7 @@ SIGNATURES = {
     "fe_sizes": [_vp, C.POINTER(_i64), C.POINTER(_i64)],
     "fe_csr_pattern": [_vp, _i32, _vp, _vp],
     "fe_residual_evaluate": [_vp, _vp, _vp, _vp],
+    "fe_residual_evaluate_noalloc": [_vp, _vp, _vp, _vp],
     "fe_jacobian_evaluate": [_vp, _vp, _vp, _vp, _vp],
     "fe_jacobian_evaluate_mixed": [_vp, _vp, _vp, _vp, _vp, _vp],
     "fe_mixed_layout": [_vp, C.POINTER(_i64), C.POINTER(_i64), _vp, _vp],

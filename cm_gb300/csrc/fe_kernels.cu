@@ -748,6 +748,30 @@ int check_batch(fe_batch b) {
 
 }  // namespace
 
+// Staging array of fe_residual_evaluate_noalloc: x in the first half, r in
+// the second.  Part of the module's device image, so using it allocates nothing.
+static __device__ __align__(256) double g_noalloc_scratch[2 * (size_t)FE_NOALLOC_MAX_DOFS];
+
+namespace {
+
+std::mutex g_noalloc_mu;           // one scratch array per device: calls are serialised
+double* g_noalloc_addr[64] = {};   // its device address, per device ordinal
+
+int noalloc_scratch(int device, double** out) {
+  if (device < 0 || device >= 64) return set_error(FE_ERR_NOT_SUPPORTED, "device ordinal out of range");
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return set_error(FE_ERR_CUDA, std::string("scratch address lookup: ") + cudaGetErrorString(e));
+    g_noalloc_addr[device] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_addr[device];
+  return FE_NO_ERROR;
+}
+
+}  // namespace
+
 namespace cmfe {
 int record_error(int code, const std::string& msg) { return set_error(code, msg); }
 }  // namespace cmfe
@@ -899,6 +923,39 @@ int fe_residual_evaluate(fe_handle h, const double* x, double* r, void* stream) 
     return finish_status(h, st);
   }
   return FE_NO_ERROR;
+}
+
+int fe_residual_evaluate_noalloc(fe_handle h, const double* x, double* r, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (!x || !r) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL x or r");
+  if (h->hs.ndofs > FE_NOALLOC_MAX_DOFS)
+    return set_error(FE_ERR_INVALID_ARGUMENT, "fe_residual_evaluate_noalloc: " + std::to_string(h->hs.ndofs) +
+                                                  " dofs exceed the static scratch limit FE_NOALLOC_MAX_DOFS = " +
+                                                  std::to_string((long long)FE_NOALLOC_MAX_DOFS));
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  std::lock_guard<std::mutex> lk(h->mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  double* base = nullptr;
+  if ((rc = noalloc_scratch(h->device, &base))) return rc;
+  double* dx = base;
+  double* dr = base + FE_NOALLOC_MAX_DOFS;
+  const size_t bytes = sizeof(double) * (size_t)h->hs.ndofs;
+  CUDA_TRY(cudaMemcpyAsync(dx, x, bytes, cudaMemcpyDefault, st));
+  KParams kp = base_params(h);
+  kp.x = dx;
+  kp.r = dr;
+  kp.res_only = 1;
+  for (int c = 0; c < h->hs.ncolours; ++c) {
+    kp.elems = h->d_colour_elems + h->hs.colour_ptr[c];
+    kp.count = h->hs.colour_ptr[c + 1] - h->hs.colour_ptr[c];
+    const int e = cmfe::launch_mixed(h->hs, kp, h->num_sms, st, h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT);
+    if (e != 0) return set_error(FE_ERR_CUDA, std::string("residual kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+    h->launches++;
+    if ((rc = surface_after(h, kp, c, 0, st))) return rc;
+  }
+  CUDA_TRY(cudaMemcpyAsync(r, dr, bytes, cudaMemcpyDefault, st));
+  return finish_status(h, st);
 }
 
 int fe_jacobian_evaluate(fe_handle h, const double* x, double* values, double* r, void* stream) {

@@ -133,6 +133,13 @@ class FiniteElasticityEquationsSet:
         check(_lib.load().fe_residual_evaluate(self._h, _ptr(x), _ptr(r), _stream(x)))
         return r
 
+    def residual_evaluate_noalloc(self, x, r=None):
+        """fe_residual_evaluate_noalloc: the residual without any device
+        allocation (static staging array; at most FE_NOALLOC_MAX_DOFS dofs)."""
+        r = np.zeros(self.ndofs) if r is None else r
+        check(_lib.load().fe_residual_evaluate_noalloc(self._h, _ptr(x), _ptr(r), _stream(x)))
+        return r
+
     def jacobian_evaluate(self, x, values=None, r=None):
         values = self._alloc_like(x, self.nnz, np.float64) if values is None else values
         check(_lib.load().fe_jacobian_evaluate(self._h, _ptr(x), _ptr(values), _ptr(r), _stream(x)))

@@ -215,6 +215,32 @@ int fe_batch_capture(fe_batch b, const double* const* x, float* const* values_uu
 int fe_batch_replay(fe_batch b, void* stream);
 int fe_batch_launch_count(fe_batch b, int64_t* count);
 
+/* ---- Residual evaluation that allocates nothing (no counterpart in the
+ * reference; same arithmetic as fe_residual_evaluate).
+ *
+ * fe_residual_evaluate given host memory stages x and r through device
+ * buffers that it allocates on its first such call; a caller that must not
+ * cause a device allocation at that point (one whose device memory is
+ * already committed, so that a cudaMalloc inside a Newton iteration could
+ * fail, or one that cannot accept the device-wide synchronisation a
+ * cudaMalloc can imply) uses this variant instead.  It stages x and r in one
+ * fixed array of 2 * FE_NOALLOC_MAX_DOFS doubles (16 MiB) that is part of the
+ * library's device image, and calls no allocating function.
+ *
+ *  - problems with more than FE_NOALLOC_MAX_DOFS dofs are rejected with
+ *    FE_ERR_INVALID_ARGUMENT;
+ *  - x and r may be host or device memory; the call returns after r is
+ *    written (it synchronises `stream`);
+ *  - nothing in the array needs to start at zero: x is copied in whole and
+ *    every residual entry is first stored, then added to, by the kernels;
+ *  - the array is shared by every handle of a device, so overlapping calls
+ *    would race on it: the library serialises them with a process-wide lock;
+ *  - the first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) and caches it, so it must come before any stream
+ *    capture that would include the call. */
+#define FE_NOALLOC_MAX_DOFS 1048576
+int fe_residual_evaluate_noalloc(fe_handle h, const double* x, double* r, void* stream);
+
 /* Waits for the handle's work on `stream` and reports numerical problems
  * seen by the kernels since the last call (FE_ERR_NUMERICAL) — the device
  * counterpart of the reference's error flags, set instead of trapping. */
