@@ -50,6 +50,11 @@ def config_mesh(name):
         m = M.regular_box(16, 16, 16, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0))
         workload = ("16x16x16 triquadratic-u/trilinear-p unit cube, MR c1=2 c2=6, "
                     "mixed-precision Jacobian + FP64 residual")
+    elif name == "cfg5":
+        m = M.guccione_slab(64, 64, 16, seed=0)
+        workload = ("64x64x16 triquadratic-u/trilinear-p slab 40x40x10 mm, Guccione C=0.88 bf=18.5 bt=3.58 "
+                    "bfs=1.63, fibre angle -60..+60 deg through the thickness +-5 deg noise, 2 kPa on z=0, "
+                    "mixed-precision Jacobian + FP64 residual")
     elif name == "cfg1":
         m = M.regular_box(4, 4, 4, nxi_u=2, pressure="element", law=M.MR, materials=(2.0, 6.0))
         workload = "4x4x4 trilinear-u/element-p unit cube, MR c1=2 c2=6, FP64 Jacobian + residual"
@@ -228,6 +233,9 @@ def our_arm(args):
     m, x, workload = config_mesh(args.config)
     mixed = args.config != "cfg1" and not args.fp64
     es = FiniteElasticityEquationsSet(m)
+    if args.config == "cfg5":
+        from cm_gb300.newton import bottom_face_pressure
+        es.set_surface_pressure(bottom_face_pressure(m, 2.0))
     dev = torch.device("cuda", local)
     xd = torch.from_numpy(x).to(dev)
     r = torch.empty(es.ndofs, dtype=torch.float64, device=dev)
@@ -373,9 +381,75 @@ def our_arm(args):
     if world == 1 and not args.no_cpu:
         rp1, col1 = es.csr_pattern(base=1)
         out["cpu_baseline"] = cpu_baseline(m, x, rp1, col1)
+    if world == 1 and args.loadstep:
+        del es, r, xd
+        torch.cuda.empty_cache()
+        out["loadstep"] = loadstep_leg(dev)
     print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
+
+
+def loadstep_leg(dev, n=8, n_train=64, n_test=4, increments=8, modes=64, train_steps=2000):
+    """Newton load-step comparison on an n^3 triquadratic box (clamped stretch
+    + shear, Mooney-Rivlin, seeded parameters as in the learned-warm-start
+    configuration): the plain method (FP64 Jacobian, reference initial guess,
+    `increments` load increments) against the mixed Jacobian started from the
+    learned prediction (one full-load increment, plain method as fallback).
+    Both reach ||r||_2 <= 1e-10 on every held-out problem."""
+    import numpy as np
+    import torch
+
+    from cm_gb300 import FiniteElasticityEquationsSet
+    from cm_gb300 import mesh as M
+    from cm_gb300 import newton as N
+    from cm_gb300 import warmstart as W
+    m = M.regular_box(n, n, n, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0), perturb=0.1, seed=2)
+    es = FiniteElasticityEquationsSet(m)
+    plain = W.ParametricProblem(es, N.NewtonOptions(linear="mg"), device=dev)
+    fast = W.ParametricProblem(es, N.NewtonOptions(linear="mg", precision="mixed"), device=dev)
+    train = W.sample_parameters(n_train, seed=21)
+    test = W.sample_parameters(n_test, seed=22)
+    t0 = time.perf_counter()
+    states, it_train = W.generate_solves(fast, train, increments, continuation=True)
+    t_data = time.perf_counter() - t0
+    ws = W.LearnedWarmStart(fast.n_pressure, modes=min(modes, n_train - 1), seed=0, device=dev)
+    rep = ws.fit(train, states, steps=train_steps, lr=2e-3, batch=min(256, n_train))
+    plain.solve_reference(test[0], increments)      # warm-up of both paths
+    fast.solve_from_state(test[0], ws.predict(test[:1])[0], increments)
+    rows = []
+    for p in test:
+        xp, rp, tp = plain.solve_reference(p, increments)
+        t1 = time.perf_counter()
+        guess = ws.predict(p[None])[0]
+        xl, rl, tl, ok = fast.solve_from_state(p, guess, increments)
+        tl = time.perf_counter() - t1
+        rows.append({"plain_iters": sum(r.iterations for r in rp), "plain_s": tp,
+                     "plain_increment_ms": 1e3 * tp / len(rp), "learned_iters": sum(r.iterations for r in rl),
+                     "learned_s": tl, "accepted": bool(ok), "converged": bool(rp[-1].converged and rl[-1].converged),
+                     "max_diff": float((xl - xp).abs().max()),
+                     "final_residual": max(rp[-1].residual_norms[-1], rl[-1].residual_norms[-1])})
+    mean = lambda k: float(np.mean([r[k] for r in rows]))  # noqa: E731
+    return {
+        "workload": "%d^3 triquadratic-u/trilinear-p box (%d dofs), clamped stretch U[1,1.3] + shear U[0,0.2], "
+                    "MR c1,c2 log-U[0.5,10]; %d held-out problems" % (n, es.ndofs, n_test),
+        "plain_fp64": {"newton_iterations": mean("plain_iters"), "solve_ms": 1e3 * mean("plain_s"),
+                       "load_step_ms": mean("plain_increment_ms"), "increments": increments,
+                       "jacobian": "FP64", "guess": "reference (current field)"},
+        "mixed_learned": {"newton_iterations": mean("learned_iters"), "solve_ms": 1e3 * mean("learned_s"),
+                          "load_step_ms": 1e3 * mean("learned_s"), "increments": 1,
+                          "jacobian": "FP32 uu (BF16x3 tensor cores) + FP64 coupling/residual",
+                          "guess": "POD-MLP prediction (BF16 tensor-core inference)",
+                          "accepted_guesses": int(sum(r["accepted"] for r in rows))},
+        "solve_speedup": mean("plain_s") / mean("learned_s"),
+        "all_converged_1e-10": all(r["converged"] and r["final_residual"] <= 1e-10 for r in rows),
+        "max_solution_difference": max(r["max_diff"] for r in rows),
+        "training": {"solves": n_train, "data_s": t_data, "mean_newton_iterations": float(it_train.mean()),
+                     "modes": rep.modes, "pod_energy": rep.energy, "train_loss": rep.train_loss,
+                     "train_s": rep.seconds},
+        "linear_solver": "GMRES + block-triangular preconditioner (multigrid V-cycle in a CUDA graph, "
+                         "scaled pressure mass)",
+    }
 
 
 def batch_arm(args):
@@ -503,10 +577,11 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="cfg2", choices=["cfg2", "cfg4", "cfg1", "cfg3"])
+    ap.add_argument("--config", default="cfg2", choices=["cfg2", "cfg4", "cfg1", "cfg3", "cfg5"])
     ap.add_argument("--batch-meshes", type=int, default=256, help="meshes in the batched configuration")
     ap.add_argument("--fp64", action="store_true", help="time the FP64 path instead of the mixed path")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--loadstep", action="store_true", help="add the Newton load-step comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

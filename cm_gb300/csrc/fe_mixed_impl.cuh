@@ -492,6 +492,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
   for (int ph = 0; ph < 2; ++ph) {
     if ((ph == 0) != p4_first) {
       // ---- P3: residual rows and pressure-coupling columns (high precision H)
+      __syncthreads();
       if (P.r != nullptr) {
         // Displacement rows by sum factorisation over the tensor-product basis:
         // r(m, a) = sum_k sum_g M_k(g; a) P_g(k, m) with M_k the product of the
@@ -652,16 +653,33 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
       // kappa = 28k + g (derivative-major, one padding slot per derivative).  Each warp owns (element, m-tile) tasks; it forms its
       // A fragments (W values) in registers from the per-Gauss-point D^{blk}
       // records and the gradient table, and takes B = Phi from shared memory.
-      {
+      if (!P.res_only) {
         constexpr int MROWS = 6 * NPE;
         constexpr int MT2 = (MROWS + 15) / 16;
         const int gq = lane >> 2, tq = lane & 3;
         const uint32_t* Bhi = s_A;
         const uint32_t* Blo = s_A + C::AROWS * KPW;
-        for (int task = warp; task < (P.res_only ? 0 : nvalid * MT2); task += C::THREADS / 32) {
+        // Scatter addresses staged in shared memory (regions P3 does not read
+        // while this stage runs): base[el][3m+n][a] = start of the n-block of
+        // row (m, node a), and the element's rank table over its u nodes.
+        int* s_base = reinterpret_cast<int*>(s_dz);
+        uint16_t* s_tab = reinterpret_cast<uint16_t*>(s_f32);
+        __syncthreads();
+        for (int i = tid; i < EG * 9 * NPE; i += C::THREADS) {
+          const int a = i % NPE, mn = (i / NPE) % 9, el = i / (9 * NPE);
+          const int na = s_node[el * (NR + 1) + a];
+          s_base[i] = el < nvalid ? P.uu_row_ptr[(size_t)(mn / 3) * nu + na] + (mn % 3) * P.wu[na] : 0;
+        }
+        for (int i = tid; i < EG * NPE * NPE; i += C::THREADS) {
+          const int ab = i % (NPE * NPE), el = i / (NPE * NPE);
+          const int a = ab / NPE, b = ab % NPE;
+          s_tab[i] = el < nvalid ? P.tables[(size_t)s_node[el * (NR + 1) + NR] * NR * NR + a * NR + b] : 0;
+        }
+        __syncthreads();
+        for (int task = warp; task < nvalid * MT2; task += C::THREADS / 32) {
           const int el = task / MT2, mt = task % MT2;
-          const int* nd = &s_node[el * (NR + 1)];
-          const uint16_t* tab = P.tables + (size_t)nd[NR] * NR * NR;
+          const int* bs = &s_base[el * 9 * NPE];
+          const uint16_t* tb = &s_tab[el * NPE * NPE];
           const float* r32 = &s_r32[el * NG * C::REC32];
           float acc[C::NT][4];
       #pragma unroll
@@ -722,16 +740,15 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
               blk_mn(blk, m, n);
               if (m == n && a < b) continue;
               const float v = acc[nt][h];
-              const int na = nd[a], nb = nd[b];
-              const uint16_t tab_ab = tab[a * NR + b];
-              const size_t p1 = (size_t)P.uu_row_ptr[(size_t)m * nu + na] + (size_t)n * P.wu[na] + (tab_ab & 0x7fff);
+              const uint16_t tab_ab = tb[a * NPE + b];
+              const int p1 = bs[(m * 3 + n) * NPE + a] + (tab_ab & 0x7fff);
               if (tab_ab & 0x8000)
                 P.vals_uu[p1] = v;
               else
                 atomicAdd(&P.vals_uu[p1], v);
               if (!(m == n && a == b)) {
-                const uint16_t tab_ba = tab[b * NR + a];
-                const size_t p2 = (size_t)P.uu_row_ptr[(size_t)n * nu + nb] + (size_t)m * P.wu[nb] + (tab_ba & 0x7fff);
+                const uint16_t tab_ba = tb[b * NPE + a];
+                const int p2 = bs[(n * 3 + m) * NPE + b] + (tab_ba & 0x7fff);
                 if (tab_ba & 0x8000)
                   P.vals_uu[p2] = v;
                 else
@@ -739,6 +756,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
               }
             }
         }
+        __syncthreads();  // P3 may run next and reuse the staging regions
       }
     }
   }

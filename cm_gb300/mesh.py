@@ -162,3 +162,18 @@ def batch_meshes(n=256, seed=0, edge_range=(4, 24), length_range=(0.5, 2.0), c_r
                                   pressure="node" if quad else "element", law=MR, materials=tuple(c)))
         stretches.append(float(rng.uniform(*stretch_range)))
     return meshes, stretches
+
+
+def guccione_slab(ex=64, ey=64, ez=16, lengths=(40.0, 40.0, 10.0), angle_range_deg=(-60.0, 60.0), noise_deg=5.0,
+                  materials=(0.88, 18.5, 3.58, 1.63), seed=0) -> Mesh:
+    """Cardiac-style slab: triquadratic displacement / trilinear nodal pressure,
+    transversely isotropic Guccione law (C, bf, bt, bfs), fibre angle varying
+    linearly through the thickness over angle_range_deg with seeded uniform
+    noise of +-noise_deg per node (imbrication and sheet angles zero)."""
+    m = regular_box(ex, ey, ez, lengths=lengths, nxi_u=3, pressure="node", law=GUCCIONE, materials=materials)
+    rng = np.random.default_rng(seed)
+    z = m.X[2] / lengths[2]
+    ang = np.deg2rad(angle_range_deg[0] + (angle_range_deg[1] - angle_range_deg[0]) * z)
+    ang = ang + np.deg2rad(rng.uniform(-noise_deg, noise_deg, size=m.nu))
+    m.fibre = np.stack([ang, np.zeros(m.nu), np.zeros(m.nu)])
+    return m

@@ -14,7 +14,8 @@ lower-triangular operator [A 0; B -S] with
   Galerkin coarse operators A_c = P^T A P on a hierarchy of regular grids
   (triquadratic -> trilinear on the element vertices, then trilinear with the
   element count halved per direction), Chebyshev smoothing on the Jacobi-
-  scaled operator, dense LU on the coarsest grid;
+  scaled operator, the inverse of the coarsest operator (dense); on the GPU
+  one V-cycle is recorded in a CUDA graph and replayed;
 * S ~ the consistent pressure mass matrix times a scale taken from
   diag(B diag(A)^-1 B^T) of the current Jacobian (the mass matrix is
   spectrally equivalent to the Schur complement for inf-sup stable pairs),
@@ -84,8 +85,9 @@ class BoxMultigrid:
 
     free_u: boolean mask over the 3*nu displacement dofs (component-major)."""
 
-    def __init__(self, grid_u, nxi_u, free_u, device, dtype=torch.float64, degree=3, min_dofs=1500):
-        self.device, self.dtype, self.degree = device, dtype, degree
+    def __init__(self, grid_u, nxi_u, free_u, device, dtype=torch.float64, degree=3, min_dofs=1500, use_graph=True):
+        self.device, self.dtype, self.degree = torch.device(device), dtype, degree
+        self.use_graph = use_graph
         self.levels = grid_hierarchy(grid_u, nxi_u, min_dofs)
         self.P, self.R = [], []
         free = np.asarray(free_u, dtype=bool)
@@ -128,8 +130,31 @@ class BoxMultigrid:
                 v = w / w.norm()
             self.lmax.append(1.1 * lam)
         Ac = self.A[-1].to_dense().to(torch.float64)
-        self.coarse_lu = torch.linalg.lu_factor(Ac)
+        self.coarse_inv = torch.linalg.inv(Ac).to(self.dtype)  # small: the coarse solve is one GEMV
+        self.graph = None
+        if self.device.type == "cuda" and self.use_graph:
+            self._capture()
         return self
+
+    def _capture(self):
+        """Records one V-cycle in a CUDA graph (static input/output buffers);
+        falls back to eager launches if the capture is refused."""
+        n = self.A[0].shape[0]
+        self.g_in = torch.zeros(n, dtype=self.dtype, device=self.device)
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            for _ in range(2):
+                self.g_out = self._vcycle(self.g_in, 0)
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        try:
+            with torch.cuda.graph(g):
+                self.g_out = self._vcycle(self.g_in, 0)
+            self.graph = g
+        except RuntimeError:
+            self.graph = None
+            torch.cuda.synchronize(self.device)
 
     @staticmethod
     def _diag(A):
@@ -162,14 +187,20 @@ class BoxMultigrid:
             rho = rho_new
         return x
 
-    def vcycle(self, b, lvl=0):
+    def vcycle(self, b):
+        if self.graph is not None:
+            self.g_in.copy_(b)
+            self.graph.replay()
+            return self.g_out.clone()
+        return self._vcycle(b, 0)
+
+    def _vcycle(self, b, lvl):
         if lvl == len(self.A) - 1:
-            x = torch.linalg.lu_solve(*self.coarse_lu, b.to(torch.float64).unsqueeze(1)).squeeze(1)
-            return x.to(b.dtype)
+            return self.coarse_inv @ b
         A = self.A[lvl]
         x = self._cheby(lvl, b, None)
         r = b - A @ x
-        x = x + self.P[lvl] @ self.vcycle(self.R[lvl] @ r, lvl + 1)
+        x = x + self.P[lvl] @ self._vcycle(self.R[lvl] @ r, lvl + 1)
         return self._cheby(lvl, b, x)
 
 

@@ -84,6 +84,26 @@ class DirichletConditions:
         return m
 
 
+class PressureIncrements:
+    """Surface pressure raised over the load increments by the reference's
+    BOUNDARY_CONDITION_PRESSURE_INCREMENTED rule
+    (equations_set_routines.f90:6652-6720): on increment 1 the applied
+    pressure is FULL / N and the previous one 0; afterwards
+    NEW = CURRENT + (CURRENT - PREVIOUS), PREVIOUS = CURRENT."""
+
+    def __init__(self, full):
+        self.full = np.asarray(full, dtype=np.float64)
+        self.current = None
+        self.previous = None
+
+    def step(self, i, n):
+        if i == 1:
+            self.current, self.previous = self.full / n, np.zeros_like(self.full)
+        else:
+            self.current, self.previous = self.current + (self.current - self.previous), self.current
+        return self.current
+
+
 class FreeDofSystem:
     """Index maps from the full CSR pattern to the free-dof submatrix."""
 
@@ -131,8 +151,13 @@ class FreeDofSystem:
         return A, B
 
 
-def _gmres(A, b, M, rtol, restart, max_it):
-    """Right-preconditioned restarted GMRES (FP64); M(v) applies the preconditioner."""
+def _gmres(A, b, M, rtol, restart, max_it, check_every=6):
+    """Right-preconditioned restarted GMRES (FP64); M(v) applies the preconditioner.
+
+    The Arnoldi process (classical Gram-Schmidt with one re-orthogonalisation)
+    stays on the device; the small least-squares problem min ||beta e1 - H y||
+    is solved on the host every `check_every` iterations to test convergence,
+    so the host waits for the device only at those points."""
     n = b.numel()
     x = torch.zeros_like(b)
     bnorm = float(b.norm())
@@ -140,49 +165,44 @@ def _gmres(A, b, M, rtol, restart, max_it):
         return x, 0
     total = 0
     r = b.clone()
+    tiny = torch.finfo(b.dtype).tiny
+    V = torch.zeros(restart + 1, n, dtype=b.dtype, device=b.device)
+    Z = torch.zeros(restart, n, dtype=b.dtype, device=b.device)
     while total < max_it:
         beta = float(r.norm())
         if beta <= rtol * bnorm:
             break
-        V = torch.zeros(restart + 1, n, dtype=b.dtype, device=b.device)
-        Z = torch.zeros(restart, n, dtype=b.dtype, device=b.device)
-        H = torch.zeros(restart + 1, restart, dtype=torch.float64)
+        H = torch.zeros(restart + 1, restart, dtype=b.dtype, device=b.device)
         V[0] = r / beta
-        g = torch.zeros(restart + 1, dtype=torch.float64)
-        g[0] = beta
-        cs = torch.zeros(restart, dtype=torch.float64)
-        sn = torch.zeros(restart, dtype=torch.float64)
         k = 0
+        y = None
         while k < restart and total < max_it:
             Z[k] = M(V[k])
             w = A @ Z[k]
-            # modified Gram-Schmidt, done as one pass of classical GS plus one refinement
             h = V[:k + 1] @ w
             w = w - V[:k + 1].T @ h
             h2 = V[:k + 1] @ w
             w = w - V[:k + 1].T @ h2
-            h = (h + h2).double().cpu()
-            hn = float(w.norm())
-            H[:k + 1, k] = h
+            hn = w.norm()
+            H[:k + 1, k] = h + h2
             H[k + 1, k] = hn
-            if hn > 0:
-                V[k + 1] = w / hn
-            for i in range(k):
-                t = cs[i] * H[i, k] + sn[i] * H[i + 1, k]
-                H[i + 1, k] = -sn[i] * H[i, k] + cs[i] * H[i + 1, k]
-                H[i, k] = t
-            d = float(torch.sqrt(H[k, k] ** 2 + H[k + 1, k] ** 2))
-            cs[k], sn[k] = H[k, k] / d, H[k + 1, k] / d
-            H[k, k] = d
-            H[k + 1, k] = 0.0
-            g[k + 1] = -sn[k] * g[k]
-            g[k] = cs[k] * g[k]
+            V[k + 1] = w / torch.clamp(hn, min=tiny)
             k += 1
             total += 1
-            if abs(float(g[k])) <= rtol * bnorm:
-                break
-        y = torch.linalg.solve_triangular(H[:k, :k], g[:k].unsqueeze(1), upper=True).squeeze(1)
-        x = x + Z[:k].T @ y.to(b.device)
+            if k % check_every == 0 or k == restart or total >= max_it:
+                Hh = H[:k + 1, :k].double().cpu()
+                rhs = torch.zeros(k + 1, dtype=torch.float64)
+                rhs[0] = beta
+                y = torch.linalg.lstsq(Hh, rhs.unsqueeze(1)).solution.squeeze(1)
+                res = float((rhs - Hh @ y).norm())
+                if res <= rtol * bnorm or float(Hh[k, k - 1]) <= 1e-14 * beta:
+                    break
+        if y is None or y.numel() != k:
+            Hh = H[:k + 1, :k].double().cpu()
+            rhs = torch.zeros(k + 1, dtype=torch.float64)
+            rhs[0] = beta
+            y = torch.linalg.lstsq(Hh, rhs.unsqueeze(1)).solution.squeeze(1)
+        x = x + Z[:k].T @ y.to(b.device, b.dtype)
         r = b - A @ x
     return x, total
 
@@ -249,7 +269,17 @@ class LoadStepSolver:
         return x
 
     def residual(self, x):
+        """Residual on the free dofs, or None when the state has an element
+        with det F <= 0 or a non-finite stress (the kernels' status word)."""
         self.es.residual_evaluate(x, self.r)
+        check = getattr(self.es, "check_status", None)
+        if check is not None:
+            try:
+                check(x)
+            except Exception as e:  # FEError(FE_ERR_NUMERICAL)
+                if getattr(e, "code", None) == -5:
+                    return None
+                raise
         return self.r[self.sys.free]
 
     def jacobian(self, x):
@@ -317,7 +347,13 @@ class LoadStepSolver:
         rep = report or StepReport()
         t_start = time.perf_counter()
         free = self.sys.free
-        r = self.residual(x).clone()
+        r = self.residual(x)
+        if r is None:
+            rep.residual_norms.append(float("inf"))
+            rep.iterations, rep.converged = 0, False
+            rep.seconds = time.perf_counter() - t_start
+            return x, rep
+        r = r.clone()
         fnorm = float(r.norm())
         rep.residual_norms.append(fnorm)
         it = 0
@@ -344,7 +380,11 @@ class LoadStepSolver:
             x0 = x[free].clone()
             while True:
                 x[free] = x0 + lam * d
-                rn = self.residual(x).clone()
+                rn = self.residual(x)
+                if rn is None:          # a step into inverted elements counts as a failed step
+                    rn = torch.full_like(r, float("inf"))
+                else:
+                    rn = rn.clone()
                 f1 = 0.5 * float(rn @ rn)
                 if np.isfinite(f1) and f1 <= f0 + o.alpha * lam * slope:
                     break
@@ -378,13 +418,17 @@ class LoadStepSolver:
         rep.seconds = time.perf_counter() - t_start
         return x, rep
 
-    def solve(self, x0, increments: int, guesses=None):
+    def solve(self, x0, increments: int, guesses=None, pressure: PressureIncrements | None = None):
         """All load increments from state x0; guesses (optional) maps the
-        increment number to a Newton initial guess for the free dofs."""
+        increment number to a Newton initial guess for the free dofs;
+        pressure (optional) raises a surface-pressure load with the
+        increments."""
         x = x0.clone()
         reports = []
         for i in range(1, increments + 1):
             x = self.apply_increment(x, i, increments)
+            if pressure is not None:
+                self.es.set_surface_pressure(pressure.step(i, increments))
             if guesses is not None and i in guesses:
                 x[self.sys.free] = guesses[i][self.sys.free]
             x, rep = self.newton(x)
@@ -435,3 +479,24 @@ def clamped_stretch_shear_conditions(mesh, stretch, shear):
 def initial_state(mesh):
     """The reference's initial dependent field: z = X, p = 0."""
     return np.concatenate([mesh.X.ravel(), np.zeros(mesh.n_pressure)])
+
+
+def clamped_lateral_conditions(mesh):
+    """Slab loading: the four lateral faces (x = 0, x = Lx, y = 0, y = Ly)
+    clamped in every component, the z faces free."""
+    i, j, k = mesh.node_ijk()
+    n1, n2, _ = mesh.grid_u
+    side = np.nonzero((i == 0) | (i == n1 - 1) | (j == 0) | (j == n2 - 1))[0]
+    bc = DirichletConditions(mesh.ndofs)
+    for c in range(3):
+        bc.fix(c * mesh.nu + side, mesh.X[c, side])
+    return bc
+
+
+def bottom_face_pressure(mesh, value):
+    """[3][nu] nodal surface pressure `value` on the z = 0 faces (faces
+    normal to xi3), zero elsewhere."""
+    i, j, k = mesh.node_ijk()
+    sp = np.zeros((3, mesh.nu))
+    sp[2, k == 0] = value
+    return sp

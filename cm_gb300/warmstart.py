@@ -318,13 +318,40 @@ def sample_parameters(n, seed, stretch=(1.0, 1.3), shear=(0.0, 0.2), c_range=(0.
     return np.stack([lam, gam, c1, c2], axis=1)
 
 
-def generate_solves(problem, params, increments):
-    """Converged free-dof states of the plain method for every parameter row."""
-    states, iters = [], []
-    for p in params:
-        x, reps, _ = problem.solve_reference(p, increments)
-        if not all(r.converged for r in reps):
+def generate_solves(problem, params, increments, continuation=False):
+    """Converged free-dof states for every parameter row.
+
+    Without continuation every row is solved by the plain method (reference
+    guess, load increments).  With continuation the rows are visited along a
+    greedy nearest-neighbour path in feature space and each solve starts from
+    the previous converged state in one increment (the plain method where
+    that fails); the converged states are the same (||r||_2 <= atol), only
+    cheaper to reach.  Returns (states in the order of params, Newton
+    iterations per row)."""
+    n = len(params)
+    order = list(range(n))
+    if continuation and n > 1:
+        f = features(params)
+        f = (f - f.mean(0)) / (f.std(0) + 1e-12)
+        left = set(range(1, n))
+        order = [0]
+        while left:
+            last = f[order[-1]]
+            nxt = min(left, key=lambda j: float(((f[j] - last) ** 2).sum()))
+            order.append(nxt)
+            left.remove(nxt)
+    states = [None] * n
+    iters = np.zeros(n, dtype=np.int64)
+    prev = None
+    for i in order:
+        p = params[i]
+        if prev is not None:
+            x, reps, _, _ = problem.solve_from_state(p, prev, increments)
+        else:
+            x, reps, _ = problem.solve_reference(p, increments)
+        if not reps[-1].converged:
             raise RuntimeError("a training solve did not converge: parameters %s" % (p,))
-        states.append(problem.state(x))
-        iters.append(sum(r.iterations for r in reps))
-    return torch.stack(states), np.array(iters)
+        states[i] = problem.state(x)
+        iters[i] = sum(r.iterations for r in reps)
+        prev = states[i] if continuation else None
+    return torch.stack(states), iters

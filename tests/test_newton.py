@@ -235,3 +235,50 @@ def test_gpu_multigrid_newton(cuda, oracle, precision):
     assert all(r.converged for r in rg)
     assert all(max(r.linear_iterations) < 80 for r in rg)
     assert float((xg - xo).abs().max()) < 1e-9
+
+
+def test_pressure_increment_rule():
+    # increment 1: FULL/N; then NEW = CUR + (CUR - PREV): a linear ramp to FULL
+    full = np.array([[0.0, 2.0], [1.0, -3.0]])
+    inc = N.PressureIncrements(full)
+    vals = [inc.step(i, 8).copy() for i in range(1, 9)]
+    for i, v in enumerate(vals, start=1):
+        assert np.allclose(v, full * i / 8, rtol=0, atol=1e-15)
+
+
+def slab_small():
+    return M.guccione_slab(3, 3, 2, lengths=(4.0, 4.0, 1.0), seed=3)
+
+
+def test_guccione_slab_pressure_newton(oracle):
+    """Guccione slab with through-thickness fibres, lateral faces clamped,
+    bottom-face pressure raised over 4 increments by the reference rule:
+    Newton converges quadratically and the slab bulges along +z."""
+    m = slab_small()
+    es = oracle.EquationsSet(m)
+    s = N.LoadStepSolver(es, N.clamped_lateral_conditions(m), N.NewtonOptions(linear="dense"), device="cpu")
+    x, reps = s.solve(torch.from_numpy(N.initial_state(m)), 4,
+                      pressure=N.PressureIncrements(N.bottom_face_pressure(m, 0.5)))
+    assert all(r.converged for r in reps) and all(r.iterations <= 8 for r in reps)
+    uz = x[2 * m.nu:3 * m.nu].numpy() - m.X[2]
+    assert uz.max() > 0.1 and uz.min() > -1e-9   # pushed along +z, nowhere pulled down
+
+
+@pytest.mark.gpu
+def test_gpu_guccione_slab_matches_oracle_newton(cuda, oracle):
+    m = slab_small()
+    bc = N.clamped_lateral_conditions(m)
+    es_o = oracle.EquationsSet(m)
+    so = N.LoadStepSolver(es_o, bc, N.NewtonOptions(linear="dense"), device="cpu")
+    xo, ro = so.solve(torch.from_numpy(N.initial_state(m)), 4,
+                      pressure=N.PressureIncrements(N.bottom_face_pressure(m, 0.5)))
+    from cm_gb300 import FiniteElasticityEquationsSet
+    es = FiniteElasticityEquationsSet(m)
+    for prec in ("fp64", "mixed"):
+        sg = N.LoadStepSolver(es, bc, N.NewtonOptions(linear="dense", precision=prec), device="cuda")
+        xg, rg = sg.solve(torch.from_numpy(N.initial_state(m)).cuda(), 4,
+                          pressure=N.PressureIncrements(N.bottom_face_pressure(m, 0.5)))
+        assert all(r.converged for r in rg)
+        if prec == "fp64":
+            assert [r.iterations for r in rg] == [r.iterations for r in ro]
+        assert float((xg.cpu() - xo).abs().max()) < 1e-9
