@@ -390,7 +390,7 @@ def our_arm(args):
         dist.destroy_process_group()
 
 
-def loadstep_leg(dev, n=8, n_train=64, n_test=4, increments=8, modes=64, train_steps=2000):
+def loadstep_leg(dev, n=8, n_train=48, n_test=4, increments=8, modes=64, train_steps=2000):
     """Newton load-step comparison on an n^3 triquadratic box (clamped stretch
     + shear, Mooney-Rivlin, seeded parameters as in the learned-warm-start
     configuration): the plain method (FP64 Jacobian, reference initial guess,
@@ -407,11 +407,11 @@ def loadstep_leg(dev, n=8, n_train=64, n_test=4, increments=8, modes=64, train_s
     m = M.regular_box(n, n, n, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0), perturb=0.1, seed=2)
     es = FiniteElasticityEquationsSet(m)
     plain = W.ParametricProblem(es, N.NewtonOptions(linear="mg"), device=dev)
-    fast = W.ParametricProblem(es, N.NewtonOptions(linear="mg", precision="mixed"), device=dev)
+    fast = W.ParametricProblem(es, N.NewtonOptions(linear="mg", precision="mixed", forcing="ew"), device=dev)
     train = W.sample_parameters(n_train, seed=21)
     test = W.sample_parameters(n_test, seed=22)
     t0 = time.perf_counter()
-    states, it_train = W.generate_solves(fast, train, increments, continuation=True)
+    states, it_train = W.generate_solves(fast, train, increments)
     t_data = time.perf_counter() - t0
     ws = W.LearnedWarmStart(fast.n_pressure, modes=min(modes, n_train - 1), seed=0, device=dev)
     rep = ws.fit(train, states, steps=train_steps, lr=2e-3, batch=min(256, n_train))
@@ -424,7 +424,9 @@ def loadstep_leg(dev, n=8, n_train=64, n_test=4, increments=8, modes=64, train_s
         guess = ws.predict(p[None])[0]
         xl, rl, tl, ok = fast.solve_from_state(p, guess, increments)
         tl = time.perf_counter() - t1
-        rows.append({"plain_iters": sum(r.iterations for r in rp), "plain_s": tp,
+        rows.append({"plain_krylov": sum(sum(r.linear_iterations) for r in rp),
+                     "learned_krylov": sum(sum(r.linear_iterations) for r in rl),
+                     "plain_iters": sum(r.iterations for r in rp), "plain_s": tp,
                      "plain_increment_ms": 1e3 * tp / len(rp), "learned_iters": sum(r.iterations for r in rl),
                      "learned_s": tl, "accepted": bool(ok), "converged": bool(rp[-1].converged and rl[-1].converged),
                      "max_diff": float((xl - xp).abs().max()),
@@ -433,14 +435,18 @@ def loadstep_leg(dev, n=8, n_train=64, n_test=4, increments=8, modes=64, train_s
     return {
         "workload": "%d^3 triquadratic-u/trilinear-p box (%d dofs), clamped stretch U[1,1.3] + shear U[0,0.2], "
                     "MR c1,c2 log-U[0.5,10]; %d held-out problems" % (n, es.ndofs, n_test),
-        "plain_fp64": {"newton_iterations": mean("plain_iters"), "solve_ms": 1e3 * mean("plain_s"),
+        "plain_fp64": {"newton_iterations": mean("plain_iters"), "krylov_iterations": mean("plain_krylov"),
+                       "solve_ms": 1e3 * mean("plain_s"),
                        "load_step_ms": mean("plain_increment_ms"), "increments": increments,
-                       "jacobian": "FP64", "guess": "reference (current field)"},
-        "mixed_learned": {"newton_iterations": mean("learned_iters"), "solve_ms": 1e3 * mean("learned_s"),
+                       "jacobian": "FP64", "guess": "reference (current field)",
+                       "krylov_tolerance": "1e-5 (reference default)"},
+        "mixed_learned": {"newton_iterations": mean("learned_iters"), "krylov_iterations": mean("learned_krylov"),
+                          "solve_ms": 1e3 * mean("learned_s"),
                           "load_step_ms": 1e3 * mean("learned_s"), "increments": 1,
                           "jacobian": "FP32 uu (BF16x3 tensor cores) + FP64 coupling/residual",
                           "guess": "POD-MLP prediction (BF16 tensor-core inference)",
-                          "accepted_guesses": int(sum(r["accepted"] for r in rows))},
+                          "accepted_guesses": int(sum(r["accepted"] for r in rows)),
+                          "krylov_tolerance": "Eisenstat-Walker forcing"},
         "solve_speedup": mean("plain_s") / mean("learned_s"),
         "all_converged_1e-10": all(r["converged"] and r["final_residual"] <= 1e-10 for r in rows),
         "max_solution_difference": max(r["max_diff"] for r in rows),
@@ -581,7 +587,8 @@ def main():
     ap.add_argument("--batch-meshes", type=int, default=256, help="meshes in the batched configuration")
     ap.add_argument("--fp64", action="store_true", help="time the FP64 path instead of the mixed path")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--loadstep", action="store_true", help="add the Newton load-step comparison")
+    ap.add_argument("--no-loadstep", dest="loadstep", action="store_false",
+                    help="skip the Newton load-step comparison (plain FP64 vs mixed + learned warm start)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

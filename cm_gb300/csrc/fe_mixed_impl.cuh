@@ -537,7 +537,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
         __syncthreads();
       }
       const int n_res = P.r != nullptr ? EG * NROW : 0;
-      const int n_cp = P.res_only ? 0 : EG * NU3;
+      const int n_cp = (P.res_only || PM) ? 0 : EG * NU3;  // nodal pressure: sum-factorised loop below
       for (int it = tid; it < n_res + n_cp; it += C::THREADS) {
         if (it < n_res) {
           const int el = it / NROW, row = it % NROW;
@@ -633,6 +633,85 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
             else
               atomicAdd(&P.vals[p2], kv);
           }
+        }
+      }
+      // Pressure-coupling block for nodal (trilinear) pressure by sum
+      // factorisation over both tensor-product bases:
+      //   K(q, n, b) = sum_k sum_g psi_q(g) A_g(k, n) dN_b/dxi_k(g),  A_g = J_z w dxi/dz,
+      // with psi_q = L(q1) L(q2) L(q3) and dN_b/dxi_k = M1k(b1) M2k(b2) M3k(b3)
+      // (M = 1-D derivative along xi_k, 1-D value otherwise), contracting
+      // g1, then g2, then g3.  One thread per (element, n, q1, b1, q2).
+      if (PM && !P.res_only) {
+        for (int t = tid; t < EG * 12 * N1; t += C::THREADS) {
+          const int q2 = t % 2, b1 = (t / 2) % N1, q1 = (t / (2 * N1)) % 2, n = (t / (4 * N1)) % 3,
+                    el = t / (12 * N1);
+          if (el >= nvalid) continue;
+          const H* rec = &s_r64[el * NG * C::REC64 + 9 + n];
+          H out[N1][2][N1];
+#pragma unroll
+          for (int b2 = 0; b2 < N1; ++b2)
+#pragma unroll
+            for (int q3 = 0; q3 < 2; ++q3)
+#pragma unroll
+              for (int b3 = 0; b3 < N1; ++b3) out[b2][q3][b3] = hval<H>(0.0);
+#pragma unroll 1
+          for (int k = 0; k < 3; ++k) {
+            const H* M1 = k == 0 ? s_D1 : s_B1;
+            const H* M2 = k == 1 ? s_D1 : s_B1;
+            const H* M3 = k == 2 ? s_D1 : s_B1;
+            H c1[3];
+#pragma unroll
+            for (int g1 = 0; g1 < 3; ++g1) c1[g1] = s_L[q1 * 3 + g1] * M1[g1 * N1 + b1];
+            H u1[9];  // g2 + 3 g3
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+              const H* tg = &rec[(3 * j) * C::REC64 + 3 * k];
+              u1[j] = hfma(c1[0], tg[0], hfma(c1[1], tg[C::REC64], c1[2] * tg[2 * C::REC64]));
+            }
+#pragma unroll
+            for (int b2 = 0; b2 < N1; ++b2) {
+              H u2[3];  // g3
+#pragma unroll
+              for (int g3 = 0; g3 < 3; ++g3) {
+                H acc = hval<H>(0.0);
+#pragma unroll
+                for (int g2 = 0; g2 < 3; ++g2) acc = hfma(s_L[q2 * 3 + g2] * M2[g2 * N1 + b2], u1[g2 + 3 * g3], acc);
+                u2[g3] = acc;
+              }
+#pragma unroll
+              for (int q3 = 0; q3 < 2; ++q3)
+#pragma unroll
+                for (int b3 = 0; b3 < N1; ++b3) {
+                  H acc = out[b2][q3][b3];
+#pragma unroll
+                  for (int g3 = 0; g3 < 3; ++g3) acc = hfma(s_L[q3 * 3 + g3] * M3[g3 * N1 + b3], u2[g3], acc);
+                  out[b2][q3][b3] = acc;
+                }
+            }
+          }
+          const int* nd = &s_node[el * (NR + 1)];
+          const uint16_t* tab = P.tables + (size_t)nd[NR] * NR * NR;
+#pragma unroll
+          for (int b2 = 0; b2 < N1; ++b2)
+#pragma unroll
+            for (int q3 = 0; q3 < 2; ++q3)
+#pragma unroll
+              for (int b3 = 0; b3 < N1; ++b3) {
+                const int q = q1 + 2 * q2 + 4 * q3, b = b1 + N1 * b2 + N1 * N1 * b3;
+                const int lq = NPE + q, pq = nd[lq], nb = nd[b];
+                const uint16_t tqb = tab[lq * NR + b], tbq = tab[b * NR + lq];
+                const double kv = hd(out[b2][q3][b3]);
+                const size_t p1 = (size_t)P.cp_row_ptr[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (tqb & 0x7fff);
+                if (tqb & 0x8000)
+                  P.vals[p1] = kv;
+                else
+                  atomicAdd(&P.vals[p1], kv);
+                const size_t p2 = (size_t)P.cp_row_ptr[(size_t)n * nu + nb] + (tbq & 0x7fff);
+                if (tbq & 0x8000)
+                  P.vals[p2] = kv;
+                else
+                  atomicAdd(&P.vals[p2], kv);
+              }
         }
       }
       // structurally zero pressure-pressure entries, stored by their first contributor

@@ -42,9 +42,10 @@ class NewtonOptions:
     linear: str = "auto"         # "dense", "gmres" (block-Jacobi), "mg" (multigrid block preconditioner)
     #                              or "auto" (dense up to dense_limit free dofs)
     dense_limit: int = 12000
-    gmres_rtol: float = 1e-6
-    gmres_restart: int = 80
+    gmres_rtol: float = 1e-5     # reference KSP defaults (solver_routines.f90:10979-10987):
+    gmres_restart: int = 30      # GMRES(30), relative tolerance 1e-5
     gmres_max_iterations: int = 600
+    forcing: str = "constant"    # "constant" (gmres_rtol) or "ew" (Eisenstat-Walker choice 2)
 
 
 @dataclass
@@ -330,15 +331,16 @@ class LoadStepSolver:
             return torch.cat([zu, zp])
         return apply
 
-    def linear_solve(self, A, b):
+    def linear_solve(self, A, b, rtol=None):
         if self.opt.linear == "dense" or (self.opt.linear == "auto" and self.sys.nf <= self.opt.dense_limit):
             D = A.to_dense()
             return torch.linalg.solve(D, b), 1
+        rtol = self.opt.gmres_rtol if rtol is None else rtol
         if self.opt.linear == "mg":
             M = self._mg_preconditioner(A)
-            return _gmres(A, b, M, self.opt.gmres_rtol, self.opt.gmres_restart, self.opt.gmres_max_iterations)
+            return _gmres(A, b, M, rtol, self.opt.gmres_restart, self.opt.gmres_max_iterations)
         M = self._preconditioner(A)
-        return _gmres(A, b, M, self.opt.gmres_rtol, self.opt.gmres_restart, self.opt.gmres_max_iterations)
+        return _gmres(A, b, M, rtol, self.opt.gmres_restart, self.opt.gmres_max_iterations)
 
     # -------------------------------------------------------------- Newton
     def newton(self, x, report: StepReport | None = None):
@@ -357,13 +359,23 @@ class LoadStepSolver:
         fnorm = float(r.norm())
         rep.residual_norms.append(fnorm)
         it = 0
+        prev_eta = None
         while fnorm > o.atol and it < o.max_iterations:
             self._sync()
             ta = time.perf_counter()
             A, _ = self.jacobian(x)
             self._sync()
             tb = time.perf_counter()
-            d, lin_it = self.linear_solve(A, -r)
+            eta = o.gmres_rtol
+            if o.forcing == "ew":
+                # Eisenstat & Walker (1996), choice 2 with gamma = 0.9, alpha = 2 and their safeguard
+                eta = 0.5 if len(rep.residual_norms) < 2 else \
+                    0.9 * (rep.residual_norms[-1] / rep.residual_norms[-2]) ** 2
+                if prev_eta is not None and 0.9 * prev_eta ** 2 > 0.1:
+                    eta = max(eta, 0.9 * prev_eta ** 2)
+                eta = min(max(eta, o.gmres_rtol), 0.5)
+                prev_eta = eta
+            d, lin_it = self.linear_solve(A, -r, eta)
             self._sync()
             rep.assembly_seconds += tb - ta
             rep.linear_seconds += time.perf_counter() - tb
