@@ -356,8 +356,9 @@ def our_arm(args):
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         try:
-            traffic = json.load(open(tp)).get(args.config + ("_mixed" if mixed else "_fp64"))
-        except (ValueError, OSError):
+            entry = json.load(open(tp)).get(args.config + ("_mixed" if mixed else "_fp64"))
+            traffic = None if entry is None else entry["bytes_per_launch"]
+        except (ValueError, OSError, KeyError, TypeError):
             traffic = None
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -371,6 +372,10 @@ def our_arm(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "traffic": traffic, "peak_source": pk["source"],
+                     "kernel": "fe_mixed_kernel" if mixed else "fe_element_kernel",
+                     "launches_per_step": launches / args.steps,
+                     "algorithmic_bytes_per_launch": B * args.steps / max(launches, 1),
+                     "traffic_unit": "DRAM bytes per launch (ncu, profiles/traffic.json)",
                      "algorithmic_bytes_per_step": B},
         "clocks": clk.summary(),
     }
