@@ -54,6 +54,7 @@ SIGNATURES = {
     "fe_destroy": [_vp],
     "fe_structure_calculate": [C.POINTER(FEMeshDesc), _i32, C.POINTER(_i64), C.POINTER(_i64), _vp, _vp],
     "fe_sizes": [_vp, C.POINTER(_i64), C.POINTER(_i64)],
+    "fe_structure_calculate_device": [C.POINTER(FEMeshDesc), _i32, C.POINTER(_i64), C.POINTER(_i64), _vp, _vp, _vp],
     "fe_csr_pattern": [_vp, _i32, _vp, _vp],
     "fe_residual_evaluate": [_vp, _vp, _vp, _vp],
     "fe_residual_evaluate_noalloc": [_vp, _vp, _vp, _vp],

@@ -48,6 +48,55 @@ def _stream(a):
     return C.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
 
 
+def mesh_desc(mesh: Mesh, keep: list):
+    """fe_mesh_desc for a mesh; the arrays it points to are appended to keep
+    (they must stay alive while the descriptor is used)."""
+    def arr(a, dt):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dt)
+        keep.append(a)
+        return a.ctypes.data
+
+    mats = np.asarray(mesh.materials, dtype=np.float64)
+    d = _lib.FEMeshDesc()
+    d.num_elements = mesh.ne
+    d.num_nodes_u = mesh.nu
+    d.num_nodes_p = mesh.np
+    d.nodes_per_xi_u = mesh.nxi_u
+    d.pressure_interpolation = mesh.p_mode
+    d.law = mesh.law
+    d.num_material_components = mats.shape[-1]
+    d.materials_per_element = 1 if mats.ndim == 2 else 0
+    d.element_nodes_u = arr(mesh.elem_u, np.int32)
+    d.element_nodes_p = arr(mesh.elem_p, np.int32)
+    d.geometry = arr(mesh.X, np.float64)
+    d.materials = arr(mats, np.float64)
+    d.fibre_angles = arr(mesh.fibre, np.float64)
+    return d
+
+
+def structure_calculate(mesh: Mesh, base: int = 0, on_device: bool = False):
+    """The Jacobian's CSR pattern of a mesh without creating an equations set:
+    fe_structure_calculate (host) or fe_structure_calculate_device (GPU).
+    Returns host (row_ptr, col) arrays."""
+    L = _lib.load()
+    keep = []
+    d = mesh_desc(mesh, keep)
+    nd, nnz = C.c_int64(), C.c_int64()
+    if on_device:
+        check(L.fe_structure_calculate_device(C.byref(d), base, C.byref(nd), C.byref(nnz), None, None, None))
+    else:
+        check(L.fe_structure_calculate(C.byref(d), base, C.byref(nd), C.byref(nnz), None, None))
+    rp = np.zeros(nd.value + 1, dtype=np.int32)
+    col = np.zeros(nnz.value, dtype=np.int32)
+    if on_device:
+        check(L.fe_structure_calculate_device(C.byref(d), base, None, None, rp.ctypes.data, col.ctypes.data, None))
+    else:
+        check(L.fe_structure_calculate(C.byref(d), base, None, None, rp.ctypes.data, col.ctypes.data))
+    return rp, col
+
+
 class FiniteElasticityEquationsSet:
     """One finite-elasticity equations set (mesh + law + materials) on the
     current CUDA device."""
@@ -56,29 +105,7 @@ class FiniteElasticityEquationsSet:
         self.mesh = mesh
         L = _lib.load()
         self._keep = []
-
-        def arr(a, dt):
-            if a is None:
-                return None
-            a = np.ascontiguousarray(a, dtype=dt)
-            self._keep.append(a)
-            return a.ctypes.data
-
-        mats = np.asarray(mesh.materials, dtype=np.float64)
-        d = _lib.FEMeshDesc()
-        d.num_elements = mesh.ne
-        d.num_nodes_u = mesh.nu
-        d.num_nodes_p = mesh.np
-        d.nodes_per_xi_u = mesh.nxi_u
-        d.pressure_interpolation = mesh.p_mode
-        d.law = mesh.law
-        d.num_material_components = mats.shape[-1]
-        d.materials_per_element = 1 if mats.ndim == 2 else 0
-        d.element_nodes_u = arr(mesh.elem_u, np.int32)
-        d.element_nodes_p = arr(mesh.elem_p, np.int32)
-        d.geometry = arr(mesh.X, np.float64)
-        d.materials = arr(mats, np.float64)
-        d.fibre_angles = arr(mesh.fibre, np.float64)
+        d = mesh_desc(mesh, self._keep)
         h = C.c_void_p()
         check(L.fe_create(C.byref(d), C.byref(h)))
         self._keep = []

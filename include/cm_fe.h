@@ -85,6 +85,14 @@ typedef struct fe_equations_set* fe_handle;
 int fe_create(const fe_mesh_desc* desc, fe_handle* out);
 int fe_destroy(fe_handle h);
 
+/* The same structure calculation on the GPU (current device): counting,
+ * sorting and de-duplicating the neighbourhood of every row node in device
+ * kernels.  Same arguments and results as fe_structure_calculate (desc
+ * arrays in host memory); row_ptr and col may be host or device memory.
+ * Synchronises `stream` before returning. */
+int fe_structure_calculate_device(const fe_mesh_desc* desc, int32_t base, int64_t* num_dofs, int64_t* nnz,
+                                  int32_t* row_ptr, int32_t* col, void* stream);
+
 /* Host-only structure calculation (no device needed): the CSR pattern the
  * set-up of fe_create builds for this mesh (JacobianMatrix_StructureCalculate,
  * equations_matrices_routines.f90:5048-5340).  num_dofs and nnz are always

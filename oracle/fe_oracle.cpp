@@ -1035,6 +1035,48 @@ int or_assemble(const OrProblem* P, const double* x, const int32_t* rp, const in
   return err ? -1 : 0;
 }
 
+// Timing sample of or_assemble: the elements first .. first+count-1 only,
+// added into values / residual (not zeroed here), element colours in order,
+// each colour's elements split over nthreads threads.
+int or_assemble_range(const OrProblem* P, const double* x, const int32_t* rp, const int32_t* ci, double* values,
+                      double* residual, int first, int count, int nthreads) {
+  const int n = or_element_size(P);
+  const int64_t nd = or_num_dofs(P);
+  const int64_t nnz = rp[nd] - 1;
+  if (first < 0 || count < 0 || first + count > P->ne) return -2;
+  std::vector<int> colour;
+  const int ncol = colour_elements(P, colour);
+  std::vector<std::vector<int>> lists(ncol);
+  for (int e = first; e < first + count; ++e) lists[colour[e]].push_back(e);
+  if (nthreads < 1) nthreads = 1;
+  int err = 0;
+  for (int c = 0; c < ncol; ++c) {
+    const std::vector<int>& L = lists[c];
+    std::vector<std::thread> th;
+    std::vector<int> errs(nthreads, 0);
+    for (int t = 0; t < nthreads; ++t)
+      th.emplace_back([&, t]() {
+        std::vector<double> Ke((size_t)n * n), re(n);
+        std::vector<int32_t> dofs(n);
+        for (size_t i = t; i < L.size(); i += nthreads) {
+          const int e = L[i];
+          or_element_dofs(P, e, dofs.data());
+          if (values) {
+            or_element_jacobian(P, e, x, Ke.data());
+            if (csr_add_element(rp, ci, nnz, values, dofs.data(), dofs.data(), n, Ke.data())) errs[t] = -1;
+          }
+          if (residual) {
+            or_element_residual(P, e, x, re.data());
+            for (int k = 0; k < n; ++k) residual[dofs[k]] = residual[dofs[k]] + re[k];
+          }
+        }
+      });
+    for (auto& h : th) h.join();
+    for (int t = 0; t < nthreads; ++t) err |= errs[t];
+  }
+  return err ? -1 : 0;
+}
+
 // ------------------------------------------------------- regular meshes ----
 // GENERATED_MESH_REGULAR_CREATE_FINISH for Lagrange tensor-product bases
 // (generated_mesh_routines.f90:1480-1600): element numbering x fastest, element

@@ -47,6 +47,8 @@ def lib():
         L.or_element_dofs.argtypes = [P, C.c_int, vp]
         L.or_pattern.argtypes = [P, vp, vp]; L.or_pattern.restype = i64
         L.or_assemble.argtypes = [P, vp, vp, vp, vp, vp, C.c_int]; L.or_assemble.restype = C.c_int
+        L.or_assemble_range.argtypes = [P, vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]
+        L.or_assemble_range.restype = C.c_int
         L.or_regular_mesh.argtypes = [C.c_int] * 4 + [vp, vp]; L.or_regular_mesh.restype = C.c_int
         L.or_basis_tables.argtypes = [C.c_int, vp, vp, vp]
         L.or_point_stress.argtypes = [C.c_int, vp, vp, C.c_double, C.c_double, vp, vp]

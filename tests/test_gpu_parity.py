@@ -294,3 +294,27 @@ def test_surface_pressure_parity(torch, oracle, name):
     P0 = oracle.Problem(m)
     _, r0 = P0.assemble(x, rp_o, col_o, jacobian=False)
     assert_entrywise(es.residual_evaluate(xd).cpu().numpy(), r0, what=name + " unloaded")
+
+
+@pytest.mark.parametrize("name", ["cfg1_lin_elem_mr", "quad_node_mr_perturbed", "lin_node_mr", "quad_elem_mr"])
+def test_device_structure_calculation_bit_exact(torch, oracle, name):
+    """fe_structure_calculate_device builds the same CSR pattern as the host
+    set-up and as the oracle's restatement of the reference rule."""
+    from cm_gb300.equations_set import structure_calculate
+    m = meshes()[name]
+    rp_h, col_h = structure_calculate(m, base=1)
+    rp_d, col_d = structure_calculate(m, base=1, on_device=True)
+    rp_o, col_o = oracle.Problem(m).pattern()
+    assert np.array_equal(rp_d, rp_h) and np.array_equal(col_d, col_h)
+    assert np.array_equal(rp_d, rp_o) and np.array_equal(col_d, col_o)
+
+
+def test_device_structure_calculation_large(torch):
+    """32^3 triquadratic box and a trilinear box: device pattern equals the
+    host pattern (0-based)."""
+    from cm_gb300.equations_set import structure_calculate
+    for m in (M.regular_box(32, 32, 32, nxi_u=3, pressure="node"),
+              M.regular_box(24, 17, 9, nxi_u=2, pressure="element")):
+        rp_h, col_h = structure_calculate(m)
+        rp_d, col_d = structure_calculate(m, on_device=True)
+        assert np.array_equal(rp_d, rp_h) and np.array_equal(col_d, col_h)
