@@ -405,7 +405,8 @@ def our_arm(args):
     if world == 1 and args.loadstep:
         del es, r, xd
         torch.cuda.empty_cache()
-        out["loadstep"] = loadstep_leg(dev)
+        out["loadstep"] = loadstep_leg(dev, n=args.loadstep_size, n_train=args.loadstep_train,
+                                       n_test=args.loadstep_test, increments=args.loadstep_increments)
     print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
@@ -608,6 +609,10 @@ def main():
     ap.add_argument("--batch-meshes", type=int, default=256, help="meshes in the batched configuration")
     ap.add_argument("--fp64", action="store_true", help="time the FP64 path instead of the mixed path")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--loadstep-size", type=int, default=8, help="elements per edge of the load-step box")
+    ap.add_argument("--loadstep-train", type=int, default=48, help="training solves of the learned warm start")
+    ap.add_argument("--loadstep-test", type=int, default=4, help="held-out problems timed")
+    ap.add_argument("--loadstep-increments", type=int, default=8, help="load increments of the plain method")
     ap.add_argument("--no-loadstep", dest="loadstep", action="store_false",
                     help="skip the Newton load-step comparison (plain FP64 vs mixed + learned warm start)")
     args = ap.parse_args()
