@@ -315,3 +315,23 @@ def test_surface_pressure_tangent_matches_fd_on_lower_blocks(oracle, nxi, pmode)
     # the surface term is present: the element Jacobian changes with the load
     P2 = oracle.Problem(m)
     assert np.abs(P.element_jacobian(0, x) - P2.element_jacobian(0, x)).max() > 1e-3
+
+
+def test_sampled_oracle_assembly_adds_up_to_the_full_assembly(oracle):
+    """or_assemble_range (the reference arm's timing sample) over windows that
+    cover the mesh gives the full or_assemble result (same colour order)."""
+    m = M.regular_box(3, 2, 2, nxi_u=3, pressure="node", perturb=0.1, seed=2)
+    x = M.deformed_state(m, stretch=1.05, shear=0.02, noise=0.02, seed=3)
+    P = oracle.Problem(m)
+    rp, col = P.pattern()
+    full_v, full_r = P.assemble(x, rp, col, nthreads=2)
+    v = np.zeros_like(full_v)
+    r = np.zeros_like(full_r)
+    L = oracle.lib()
+    for first in range(0, m.ne, 5):
+        n = min(5, m.ne - first)
+        assert L.or_assemble_range(P.ref, x.ctypes.data, rp.ctypes.data, col.ctypes.data, v.ctypes.data,
+                                   r.ctypes.data, first, n, 2) == 0
+    S = np.abs(full_v).max()
+    assert np.abs(v - full_v).max() <= 1e-13 * S
+    assert np.abs(r - full_r).max() <= 1e-13 * np.abs(full_r).max()
