@@ -7,7 +7,7 @@
 namespace {
 
 template <int N1, int PM, int SPLIT, class H>
-__global__ void __launch_bounds__(256, 2) fe_mixed_kernel(KParams P) {
+__global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB) fe_mixed_kernel(KParams P) {
   using C = MixCfg<N1, PM>;
   extern __shared__ __align__(16) unsigned char sm[];
   mix_tables<N1, PM, C::EG, H>(P, sm);

@@ -46,8 +46,14 @@ namespace {
 
 constexpr int align16(int x) { return (x + 15) & ~15; }
 
-template <int N1, int PM, int EG_ = (N1 == 3 ? 4 : 8)>
+// Default elements per group: 3 for triquadratic elements with nodal pressure
+// (about 72 KB of shared memory, so three 256-thread CTAs fit on an SM, which
+// measured 17 % faster than two CTAs of 4 elements despite the register
+// spills the 80-register budget causes), 4 for element-based pressure (which
+// also keeps the FP64 gradient table), 8 for trilinear elements.
+template <int N1, int PM, int EG_ = (N1 == 3 ? (PM ? 3 : 4) : 8)>
 struct MixCfg {
+  static constexpr int MINB = (N1 == 3 && PM) ? 3 : 2;  // CTAs per SM the launch bounds ask for
   static constexpr int NPE = N1 * N1 * N1;
   static constexpr int NPP = PM ? 8 : 1;
   static constexpr int NR = NPE + NPP;
@@ -66,7 +72,7 @@ struct MixCfg {
   static constexpr int PHS = 84;    // per-Gauss-point stride of the FP32 gradient table (conflict-free fragment loads)
   static constexpr int KAP = 84;    // contraction length: kappa = 28 k + g, g < 27 (g = 27 is padding)
   static constexpr int O_PHI64 = 0;
-  static constexpr int O_PSI64 = align16(O_PHI64 + NG * 4 * NPE * 8);
+  static constexpr int O_PSI64 = align16(O_PHI64 + (PM ? 0 : NG * 4 * NPE * 8));  // FP64 gradient table: element-based pressure only
   static constexpr int O_L = align16(O_PSI64 + NG * 8 * 8);
   static constexpr int O_W = align16(O_L + 6 * 8);
   static constexpr int O_1D = align16(O_W + NG * 8);
@@ -220,7 +226,8 @@ __device__ __forceinline__ void mix_tables(const KParams& P, unsigned char* sm) 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nu = P.nu;
   // ---- constant tables
-  for (int i = tid; i < NG * 4 * NPE; i += C::THREADS) s_phi[i] = hval<H>(P.gbf_u[i]);
+  if (!PM)  // read only by the element-based pressure coupling
+    for (int i = tid; i < NG * 4 * NPE; i += C::THREADS) s_phi[i] = hval<H>(P.gbf_u[i]);
   for (int i = tid; i < NG * 8; i += C::THREADS) s_psi[i] = hval<H>(P.gbf_p[i]);
   for (int i = tid; i < NG; i += C::THREADS) s_w[i] = hval<H>(P.gw[i]);
   if (tid < 6) {
