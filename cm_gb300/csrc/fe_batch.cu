@@ -83,8 +83,8 @@ __device__ __forceinline__ void run_group(int type, const KParams& P, int grp, b
   }
 }
 
-template <int EGQ, int EGL, class H>
-__global__ void __launch_bounds__(BT_THREADS, 2) fe_mixed_batch_kernel(BatchArgs A) {
+template <int EGQ, int EGL, int MINB, class H>
+__global__ void __launch_bounds__(BT_THREADS, MINB) fe_mixed_batch_kernel(BatchArgs A) {
   using B = BatchCfg<EGQ, EGL>;
   extern __shared__ __align__(16) unsigned char sm[];
   KParams* kp = reinterpret_cast<KParams*>(sm);
@@ -122,17 +122,18 @@ __global__ void __launch_bounds__(BT_THREADS, 2) fe_mixed_batch_kernel(BatchArgs
 }
 
 // Launch variants the autotuner chooses from: elements per group for
-// triquadratic / trilinear members.
+// triquadratic / trilinear members, and the CTAs per SM the register budget
+// is compiled for (3 = 80 registers, some spills; 2 = 128).
 struct Variant {
-  int egq, egl;
+  int egq, egl, minb;
 };
-constexpr Variant VARIANTS[] = {{4, 8}, {4, 4}, {2, 4}, {2, 2}};
-constexpr int NVARIANTS = 4;
+constexpr Variant VARIANTS[] = {{4, 8, 2}, {4, 4, 2}, {2, 4, 2}, {2, 2, 2}, {3, 2, 3}};
+constexpr int NVARIANTS = 5;
 
-template <int EGQ, int EGL>
+template <int EGQ, int EGL, int MINB = 2>
 int launch_variant(const BatchArgs& a, int ctas_per_sm, int num_sms, cudaStream_t st, int* grid_out) {
   using B = BatchCfg<EGQ, EGL>;
-  auto kern = fe_mixed_batch_kernel<EGQ, EGL, double>;
+  auto kern = fe_mixed_batch_kernel<EGQ, EGL, MINB, double>;
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, B::SMEM);
@@ -171,7 +172,8 @@ int batch_smem(int v) {
     case 0: return BatchCfg<4, 8>::SMEM;
     case 1: return BatchCfg<4, 4>::SMEM;
     case 2: return BatchCfg<2, 4>::SMEM;
-    default: return BatchCfg<2, 2>::SMEM;
+    case 3: return BatchCfg<2, 2>::SMEM;
+    default: return BatchCfg<3, 2>::SMEM;
   }
 }
 
@@ -181,7 +183,8 @@ int launch_mixed_batch(int variant, const BatchArgs& a, int ctas_per_sm, int num
     case 0: return launch_variant<4, 8>(a, ctas_per_sm, num_sms, st, nullptr);
     case 1: return launch_variant<4, 4>(a, ctas_per_sm, num_sms, st, nullptr);
     case 2: return launch_variant<2, 4>(a, ctas_per_sm, num_sms, st, nullptr);
-    default: return launch_variant<2, 2>(a, ctas_per_sm, num_sms, st, nullptr);
+    case 3: return launch_variant<2, 2>(a, ctas_per_sm, num_sms, st, nullptr);
+    default: return launch_variant<3, 2, 3>(a, ctas_per_sm, num_sms, st, nullptr);
   }
 }
 

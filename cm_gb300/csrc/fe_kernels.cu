@@ -1265,7 +1265,7 @@ int fe_batch_autotune(fe_batch b, const double* const* x, float* const* values_u
   int bv = keep_v, bc = keep_c, bb = keep_b;
   const int blocks[] = {1, 2, 4};
   for (int v = 0; v < cmfe::batch_variants() && !rc; ++v)
-    for (int cps = 1; cps <= 2 && !rc; ++cps) {
+    for (int cps = 1; cps <= 3 && !rc; ++cps) {
       // skip a CTA count the shared memory cannot hold (the launch would use fewer)
       if (cps * (cmfe::batch_smem(v) + 1024) > 232448) continue;
       for (int bg : blocks) {

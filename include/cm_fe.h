@@ -205,7 +205,8 @@ int fe_batch_jacobian_evaluate_mixed(fe_batch b, const double* const* x, float* 
 int fe_batch_check(fe_batch b, void* stream);
 
 /* Launch configuration: variant (elements per group for triquadratic /
- * trilinear members: 0 = 4/8, 1 = 4/4, 2 = 2/4, 3 = 2/2), CTAs per SM, and
+ * trilinear members: 0 = 4/8, 1 = 4/4, 2 = 2/4, 3 = 2/2, 4 = 3/2 compiled for
+ * three CTAs per SM), CTAs per SM, and
  * element groups per work item (the colour-block size). */
 int fe_batch_set_config(fe_batch b, int32_t variant, int32_t ctas_per_sm, int32_t block_groups);
 int fe_batch_get_config(fe_batch b, int32_t* variant, int32_t* ctas_per_sm, int32_t* block_groups,

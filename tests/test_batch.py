@@ -65,7 +65,7 @@ def _close(torch, refs, vus, vcs, rs):
 def test_batch_matches_single_set_bitwise(torch):
     sets, xs, refs, batch = _setup(torch)
     vus, vcs, rs = batch.allocate("cuda")
-    for variant in range(4):
+    for variant in range(5):
         for cps in (1, 2):
             for bg in (1, 3):
                 batch.set_config(variant, cps, bg)
@@ -78,14 +78,14 @@ def test_batch_matches_single_set_bitwise(torch):
                 batch.jacobian_evaluate_mixed(xs, vus, vcs, rs)
                 batch.check(xs[0])
                 assert all(torch.equal(a, b) for a, b in zip(first, vus + vcs + rs))
-    assert batch.launch_count() == 32
+    assert batch.launch_count() == 40
 
 
 def test_autotune_and_graph_replay(torch):
     sets, xs, refs, batch = _setup(torch)
     vus, vcs, rs = batch.allocate("cuda")
     cfg = batch.autotune(xs, vus, vcs, rs, repeats=2)
-    assert 0 <= cfg["variant"] < 4 and cfg["tuned_ms"] > 0
+    assert 0 <= cfg["variant"] < 5 and cfg["tuned_ms"] > 0
     batch.capture(xs, vus, vcs, rs)
     for t in vus + vcs + rs:
         t.zero_()
