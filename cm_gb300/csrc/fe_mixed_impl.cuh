@@ -515,7 +515,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
           const H* M = k == 0 ? s_D1 : s_B1;
           const H* rec = &s_r64[(el * NG + 3 * j) * C::REC64 + k * 3 + m];
           H acc = hval<H>(0.0);
-      #pragma unroll
+#pragma unroll
           for (int g1 = 0; g1 < 3; ++g1) acc = hfma(M[g1 * N1 + a1], rec[g1 * C::REC64], acc);
           U1[i] = acc;
         }
@@ -526,7 +526,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
           const H* M = mk % 3 == 1 ? s_D1 : s_B1;
           const H* u = &U1[((el * 9 + mk) * N1 + a1) * 9 + 3 * g3];
           H acc = hval<H>(0.0);
-      #pragma unroll
+#pragma unroll
           for (int g2 = 0; g2 < 3; ++g2) acc = hfma(M[g2 * N1 + a2], u[g2], acc);
           U2[i] = acc;
         }
@@ -537,7 +537,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
           const H* M = mk % 3 == 2 ? s_D1 : s_B1;
           const H* u = &U2[((el * 9 + mk) * N2 + a12) * 3];
           H acc = hval<H>(0.0);
-      #pragma unroll
+#pragma unroll
           for (int g3 = 0; g3 < 3; ++g3) acc = hfma(M[g3 * N1 + a3], u[g3], acc);
           RK[i] = acc;
         }
@@ -587,10 +587,10 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
           H Kq[NPP];
           H s1[2][9];
           H vsum = hval<H>(0.0);
-      #pragma unroll
+#pragma unroll
           for (int jj = 0; jj < 9; ++jj) {
             H v3[3];
-      #pragma unroll
+#pragma unroll
             for (int g1 = 0; g1 < 3; ++g1) {
               const int g = g1 + 3 * jj;
               const H* ph = &s_phi[g * 4 * NPE + b];
@@ -598,7 +598,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
               v3[g1] = hfma(rg[n], ph[NPE], hfma(rg[3 + n], ph[2 * NPE], rg[6 + n] * ph[3 * NPE]));
             }
             if (PM) {
-      #pragma unroll
+#pragma unroll
               for (int q1 = 0; q1 < 2; ++q1)
                 s1[q1][jj] = hfma(s_L[q1 * 3], v3[0], hfma(s_L[q1 * 3 + 1], v3[1], s_L[q1 * 3 + 2] * v3[2]));
             } else {
@@ -607,15 +607,15 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
           }
           if (PM) {
             H s2[2][2][3];
-      #pragma unroll
+#pragma unroll
             for (int q1 = 0; q1 < 2; ++q1)
-      #pragma unroll
+#pragma unroll
               for (int q2 = 0; q2 < 2; ++q2)
-      #pragma unroll
+#pragma unroll
                 for (int g3 = 0; g3 < 3; ++g3)
                   s2[q1][q2][g3] = hfma(s_L[q2 * 3], s1[q1][3 * g3],
                                         hfma(s_L[q2 * 3 + 1], s1[q1][3 * g3 + 1], s_L[q2 * 3 + 2] * s1[q1][3 * g3 + 2]));
-      #pragma unroll
+#pragma unroll
             for (int q = 0; q < NPP; ++q) {
               const int q1 = q & 1, q2 = (q >> 1) & 1, q3 = q >> 2;
               Kq[q] = hfma(s_L[q3 * 3], s2[q1][q2][0], hfma(s_L[q3 * 3 + 1], s2[q1][q2][1], s_L[q3 * 3 + 2] * s2[q1][q2][2]));
@@ -624,7 +624,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
             Kq[0] = vsum;
           }
           const int nb = nd[b];
-      #pragma unroll
+#pragma unroll
           for (int q = 0; q < NPP; ++q) {
             const int lq = NPE + q, pq = nd[lq];
             const uint16_t tqb = tab[lq * NR + b], tbq = tab[b * NR + lq];
@@ -768,17 +768,17 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
           const uint16_t* tb = &s_tab[el * NPE * NPE];
           const float* r32 = &s_r32[el * NG * C::REC32];
           float acc[C::NT][4];
-      #pragma unroll
+#pragma unroll
           for (int nt = 0; nt < C::NT; ++nt)
-      #pragma unroll
+#pragma unroll
             for (int h = 0; h < 4; ++h) acc[nt][h] = 0.f;
           const int R0 = 16 * mt + gq, R1 = R0 + 8;
           const int blk0 = R0 / NPE, b0 = R0 % NPE, blk1 = R1 / NPE, b1 = R1 % NPE;
           const bool v0 = R0 < MROWS, v1 = R1 < MROWS;
-      #pragma unroll 1
+#pragma unroll 1
           for (int kt = 0; kt < C::KT; ++kt) {
             float wv[2][4];  // [row r0/r1][kappa 2t, 2t+1, 2t+8, 2t+9]
-      #pragma unroll
+#pragma unroll
             for (int j = 0; j < 4; ++j) {
               const int kap = 16 * kt + 2 * tq + (j & 1) + (j >= 2 ? 8 : 0);
               const int k = kap / 28, g = kap % 28;
@@ -802,7 +802,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
             split_bf16(wv[1][0], wv[1][1], ah[1], al[1]);  // row r1, cols 2t..2t+1
             split_bf16(wv[0][2], wv[0][3], ah[2], al[2]);  // row r0, cols 2t+8..
             split_bf16(wv[1][2], wv[1][3], ah[3], al[3]);  // row r1, cols 2t+8..
-      #pragma unroll
+#pragma unroll
             for (int nt = 0; nt < C::NT; ++nt) {
               const int rb = (8 * nt + gq) * KPW, c0 = 8 * kt + tq, c1 = c0 + 4;
               const uint32_t bh0 = Bhi[rb + c0], bh1 = Bhi[rb + c1];
@@ -814,9 +814,9 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
             }
           }
           // scatter K^{blk}(a, b) and its mirror
-      #pragma unroll
+#pragma unroll
           for (int nt = 0; nt < C::NT; ++nt)
-      #pragma unroll
+#pragma unroll
             for (int h = 0; h < 4; ++h) {
               const bool vr = h < 2 ? v0 : v1;
               const int blk = h < 2 ? blk0 : blk1, b = h < 2 ? b0 : b1;
