@@ -405,11 +405,56 @@ def our_arm(args):
     if world == 1 and args.loadstep:
         del es, r, xd
         torch.cuda.empty_cache()
-        out["loadstep"] = loadstep_leg(dev, n=args.loadstep_size, n_train=args.loadstep_train,
-                                       n_test=args.loadstep_test, increments=args.loadstep_increments)
+        if args.config == "cfg5":
+            out["loadstep"] = slab_newton_leg(dev)
+        else:
+            out["loadstep"] = loadstep_leg(dev, n=args.loadstep_size, n_train=args.loadstep_train,
+                                           n_test=args.loadstep_test, increments=args.loadstep_increments)
     print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
+
+
+def slab_newton_leg(dev, ex=16, ey=16, ez=4, increments=8, pressure=2.0):
+    """Newton with the reference's pressure-increment rule on a Guccione slab
+    (the slab configuration at reduced resolution: 40x40x10 mm, fibres -60..+60
+    degrees through the thickness, lateral faces clamped, cavity pressure on
+    z = 0 raised to `pressure` kPa over `increments` increments): plain FP64
+    Jacobian against the mixed Jacobian, both to ||r||_2 <= 1e-10."""
+    import torch
+
+    from cm_gb300 import FiniteElasticityEquationsSet
+    from cm_gb300 import mesh as M
+    from cm_gb300 import newton as N
+    m = M.guccione_slab(ex, ey, ez, seed=0)
+    es = FiniteElasticityEquationsSet(m)
+    bc = N.clamped_lateral_conditions(m)
+    full = N.bottom_face_pressure(m, pressure)
+    x0 = torch.from_numpy(N.initial_state(m)).to(dev)
+    res = {}
+    xs = {}
+    for name, opt in (("plain_fp64", N.NewtonOptions(linear="mg")),
+                      ("mixed", N.NewtonOptions(linear="mg", precision="mixed", forcing="ew"))):
+        s = N.LoadStepSolver(es, bc, opt, device=dev)
+        s.solve(x0, 1, pressure=N.PressureIncrements(full / increments))   # warm-up (graph capture, tables)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        x, reps = s.solve(x0, increments, pressure=N.PressureIncrements(full))
+        torch.cuda.synchronize(dev)
+        dt = time.perf_counter() - t0
+        xs[name] = x
+        uz = (x[2 * m.nu:3 * m.nu].cpu().numpy() - m.X[2])
+        res[name] = {"newton_iterations": sum(r.iterations for r in reps),
+                     "krylov_iterations": sum(sum(r.linear_iterations) for r in reps),
+                     "solve_ms": 1e3 * dt, "load_step_ms": 1e3 * dt / max(len(reps), 1),
+                     "increments_done": len(reps), "converged": all(r.converged for r in reps),
+                     "final_residual": reps[-1].residual_norms[-1], "max_uz_mm": float(uz.max())}
+    res["workload"] = ("%dx%dx%d triquadratic Guccione slab 40x40x10 mm (%d dofs), lateral faces clamped, "
+                       "%.1f kPa on z=0 in %d increments (reference pressure-increment rule)"
+                       % (ex, ey, ez, es.ndofs, pressure, increments))
+    res["solve_speedup"] = res["plain_fp64"]["solve_ms"] / res["mixed"]["solve_ms"]
+    res["max_solution_difference"] = float((xs["plain_fp64"] - xs["mixed"]).abs().max())
+    return res
 
 
 def loadstep_leg(dev, n=8, n_train=48, n_test=4, increments=8, modes=64, train_steps=2000):
