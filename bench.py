@@ -415,46 +415,67 @@ def our_arm(args):
         dist.destroy_process_group()
 
 
-def slab_newton_leg(dev, ex=16, ey=16, ez=4, increments=8, pressure=2.0):
+def slab_newton_leg(dev, ex=16, ey=16, ez=4, increments=8, n_train=48, n_test=4):
     """Newton with the reference's pressure-increment rule on a Guccione slab
     (the slab configuration at reduced resolution: 40x40x10 mm, fibres -60..+60
     degrees through the thickness, lateral faces clamped, cavity pressure on
-    z = 0 raised to `pressure` kPa over `increments` increments): plain FP64
-    Jacobian against the mixed Jacobian, both to ||r||_2 <= 1e-10."""
+    z = 0), over seeded (pressure in [0.25, 2] kPa, C log-uniform in [0.5, 2]
+    kPa): the plain method (FP64 Jacobian, `increments` pressure increments)
+    against the mixed Jacobian started from the learned prediction (the full
+    pressure at once, plain method as fallback), all to ||r||_2 <= 1e-10."""
+    import numpy as np
     import torch
 
     from cm_gb300 import FiniteElasticityEquationsSet
     from cm_gb300 import mesh as M
     from cm_gb300 import newton as N
+    from cm_gb300 import warmstart as W
     m = M.guccione_slab(ex, ey, ez, seed=0)
     es = FiniteElasticityEquationsSet(m)
-    bc = N.clamped_lateral_conditions(m)
-    full = N.bottom_face_pressure(m, pressure)
-    x0 = torch.from_numpy(N.initial_state(m)).to(dev)
-    res = {}
-    xs = {}
-    for name, opt in (("plain_fp64", N.NewtonOptions(linear="mg")),
-                      ("mixed", N.NewtonOptions(linear="mg", precision="mixed", forcing="ew"))):
-        s = N.LoadStepSolver(es, bc, opt, device=dev)
-        s.solve(x0, 1, pressure=N.PressureIncrements(full / increments))   # warm-up (graph capture, tables)
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        x, reps = s.solve(x0, increments, pressure=N.PressureIncrements(full))
-        torch.cuda.synchronize(dev)
-        dt = time.perf_counter() - t0
-        xs[name] = x
-        uz = (x[2 * m.nu:3 * m.nu].cpu().numpy() - m.X[2])
-        res[name] = {"newton_iterations": sum(r.iterations for r in reps),
-                     "krylov_iterations": sum(sum(r.linear_iterations) for r in reps),
-                     "solve_ms": 1e3 * dt, "load_step_ms": 1e3 * dt / max(len(reps), 1),
-                     "increments_done": len(reps), "converged": all(r.converged for r in reps),
-                     "final_residual": reps[-1].residual_norms[-1], "max_uz_mm": float(uz.max())}
-    res["workload"] = ("%dx%dx%d triquadratic Guccione slab 40x40x10 mm (%d dofs), lateral faces clamped, "
-                       "%.1f kPa on z=0 in %d increments (reference pressure-increment rule)"
-                       % (ex, ey, ez, es.ndofs, pressure, increments))
-    res["solve_speedup"] = res["plain_fp64"]["solve_ms"] / res["mixed"]["solve_ms"]
-    res["max_solution_difference"] = float((xs["plain_fp64"] - xs["mixed"]).abs().max())
-    return res
+    plain = W.SlabProblem(es, N.NewtonOptions(linear="mg"), device=dev)
+    fast = W.SlabProblem(es, N.NewtonOptions(linear="mg", precision="mixed", forcing="ew"), device=dev)
+    train = W.sample_slab_parameters(n_train, seed=41)
+    test = W.sample_slab_parameters(n_test, seed=42)
+    t0 = time.perf_counter()
+    states, it_train = W.generate_solves(fast, train, increments)
+    t_data = time.perf_counter() - t0
+    ws = W.LearnedWarmStart(fast.n_pressure, modes=min(64, n_train - 1), seed=0, device=dev,
+                            featurize=W.slab_features)
+    rep = ws.fit(train, states, steps=2000, lr=2e-3, batch=min(256, n_train))
+    plain.solve_reference(test[0], increments)      # warm-up of both paths
+    fast.solve_from_state(test[0], ws.predict(test[:1])[0], increments)
+    rows = []
+    for p in test:
+        xp, rp, tp = plain.solve_reference(p, increments)
+        t1 = time.perf_counter()
+        guess = ws.predict(p[None])[0]
+        xl, rl, _, ok = fast.solve_from_state(p, guess, increments)
+        tl = time.perf_counter() - t1
+        uz = (xp[2 * m.nu:3 * m.nu].cpu().numpy() - m.X[2])
+        rows.append({"plain_iters": sum(r.iterations for r in rp), "plain_krylov": sum(sum(r.linear_iterations) for r in rp),
+                     "plain_s": tp, "learned_iters": sum(r.iterations for r in rl),
+                     "learned_krylov": sum(sum(r.linear_iterations) for r in rl), "learned_s": tl, "accepted": bool(ok),
+                     "converged": bool(rp[-1].converged and rl[-1].converged),
+                     "final_residual": max(rp[-1].residual_norms[-1], rl[-1].residual_norms[-1]),
+                     "max_diff": float((xl - xp).abs().max()), "max_uz": float(uz.max())})
+    mean = lambda k: float(np.mean([r[k] for r in rows]))  # noqa: E731
+    return {
+        "workload": ("%dx%dx%d triquadratic Guccione slab 40x40x10 mm (%d dofs), lateral faces clamped, cavity "
+                     "pressure U[0.25,2] kPa on z=0, C log-U[0.5,2] kPa; %d held-out problems"
+                     % (ex, ey, ez, es.ndofs, n_test)),
+        "plain_fp64": {"newton_iterations": mean("plain_iters"), "krylov_iterations": mean("plain_krylov"),
+                       "solve_ms": 1e3 * mean("plain_s"), "load_step_ms": 1e3 * mean("plain_s") / increments,
+                       "increments": increments, "guess": "reference (current field)"},
+        "mixed_learned": {"newton_iterations": mean("learned_iters"), "krylov_iterations": mean("learned_krylov"),
+                          "solve_ms": 1e3 * mean("learned_s"), "load_step_ms": 1e3 * mean("learned_s"),
+                          "increments": 1, "accepted_guesses": int(sum(r["accepted"] for r in rows))},
+        "solve_speedup": mean("plain_s") / mean("learned_s"),
+        "all_converged_1e-10": all(r["converged"] and r["final_residual"] <= 1e-10 for r in rows),
+        "max_solution_difference": max(r["max_diff"] for r in rows),
+        "max_deflection_mm": max(r["max_uz"] for r in rows),
+        "training": {"solves": n_train, "data_s": t_data, "mean_newton_iterations": float(it_train.mean()),
+                     "modes": rep.modes, "train_loss": rep.train_loss, "train_s": rep.seconds},
+    }
 
 
 def loadstep_leg(dev, n=8, n_train=48, n_test=4, increments=8, modes=64, train_steps=2000):

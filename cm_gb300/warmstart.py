@@ -211,8 +211,9 @@ class TrainReport:
 class LearnedWarmStart:
     """Maps (stretch, shear, c1, c2) to the free-dof state [z - X; p]."""
 
-    def __init__(self, n_pressure, modes=64, hidden=(256, 256, 256), seed=0, device="cuda"):
+    def __init__(self, n_pressure, modes=64, hidden=(256, 256, 256), seed=0, device="cuda", featurize=None):
         self.n_p = int(n_pressure)   # trailing pressure entries of a state
+        self.featurize = featurize or features  # parameters -> network inputs
         self.r = modes
         self.hidden = hidden
         self.seed = seed
@@ -236,19 +237,19 @@ class LearnedWarmStart:
         coef = self.pod.coefficients(S)
         rec = self.pod.reconstruct(coef) * self.scale
         pod_err = float(((rec - states).norm(dim=1) / states.norm(dim=1).clamp(min=1e-300)).max())
-        f = features(params)
+        f = self.featurize(params)
         self.f_mean, self.f_std = f.mean(0), f.std(0) + 1e-12
         x = torch.from_numpy((f - self.f_mean) / self.f_std).to(self.device, torch.float32)
         self.c_std = coef.std(0).clamp(min=1e-300)
         y = (coef / self.c_std).to(torch.float32)
-        self.net = MLP((4,) + tuple(self.hidden) + (r,), seed=self.seed, device=self.device)
+        self.net = MLP((f.shape[1],) + tuple(self.hidden) + (r,), seed=self.seed, device=self.device)
         loss = self.net.fit(x, y, steps=steps, lr=lr, batch=batch, seed=self.seed)
         torch.cuda.synchronize(self.device)
         return TrainReport(samples=S.shape[0], modes=r, energy=self.pod.energy, train_loss=loss,
                            seconds=time.perf_counter() - t0, pod_relative_error=pod_err)
 
     def predict(self, params, bf16=True):
-        f = features(params)
+        f = self.featurize(params)
         x = torch.from_numpy((f - self.f_mean) / self.f_std).to(self.device, torch.float32)
         y = self.net.infer_bf16(x) if bf16 else self.net.forward(x)[-1]
         coef = y.to(torch.float64) * self.c_std
@@ -355,3 +356,72 @@ def generate_solves(problem, params, increments, continuation=False):
         iters[i] = sum(r.iterations for r in reps)
         prev = states[i] if continuation else None
     return torch.stack(states), iters
+
+
+def slab_features(params):
+    """(surface pressure, Guccione C) -> (pressure, log C)."""
+    p = np.asarray(params, dtype=np.float64)
+    return np.stack([p[:, 0], np.log(p[:, 1])], axis=1)
+
+
+def sample_slab_parameters(n, seed, pressure=(0.25, 2.0), c_range=(0.5, 2.0)):
+    """Seeded (cavity pressure in kPa, Guccione C in kPa): pressure uniform,
+    C log-uniform."""
+    rng = np.random.default_rng(seed)
+    return np.stack([rng.uniform(*pressure, size=n), np.exp(rng.uniform(*np.log(c_range), size=n))], axis=1)
+
+
+class SlabProblem:
+    """The cardiac-style slab over (cavity pressure, Guccione C): lateral faces
+    clamped, the pressure on z = 0 raised over the increments by the
+    reference's pressure-increment rule; one equations set and solver reused
+    for every sample (the other Guccione constants stay those of the mesh)."""
+
+    def __init__(self, es, options, device="cuda"):
+        from . import newton as N
+        self.N = N
+        self.es = es
+        self.mesh = es.mesh
+        self.device = torch.device(device)
+        self.base_materials = np.asarray(self.mesh.materials, dtype=np.float64).copy()
+        self.solver = N.LoadStepSolver(es, N.clamped_lateral_conditions(self.mesh), options, device=self.device)
+        self.x_init = torch.from_numpy(N.initial_state(self.mesh)).to(self.device)
+        self.free = self.solver.sys.free
+        self.n_pressure = self.solver.sys.nfp
+
+    def set_parameters(self, p):
+        mats = self.base_materials.copy()
+        mats[0] = float(p[1])
+        self.es.set_materials(mats)
+
+    def state(self, x):
+        return x[self.free] - self.x_init[self.free]
+
+    def _sync(self):
+        if self.device.type == "cuda":
+            torch.cuda.synchronize(self.device)
+
+    def solve_reference(self, p, increments):
+        self.set_parameters(p)
+        t0 = time.perf_counter()
+        full = self.N.bottom_face_pressure(self.mesh, float(p[0]))
+        x, reps = self.solver.solve(self.x_init, increments, pressure=self.N.PressureIncrements(full))
+        self._sync()
+        return x, reps, time.perf_counter() - t0
+
+    def solve_from_state(self, p, state, fallback_increments):
+        """The full pressure at once from a predicted state; the reference
+        method if that does not converge."""
+        self.set_parameters(p)
+        t0 = time.perf_counter()
+        self.es.set_surface_pressure(self.N.bottom_face_pressure(self.mesh, float(p[0])))
+        x = self.x_init.clone()
+        x[self.free] = self.x_init[self.free] + state
+        x, rep = self.solver.newton(x)
+        if rep.converged:
+            self._sync()
+            return x, [rep], time.perf_counter() - t0, True
+        full = self.N.bottom_face_pressure(self.mesh, float(p[0]))
+        x, reps = self.solver.solve(self.x_init, fallback_increments, pressure=self.N.PressureIncrements(full))
+        self._sync()
+        return x, [rep] + reps, time.perf_counter() - t0, False

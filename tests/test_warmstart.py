@@ -170,3 +170,47 @@ def test_learned_warm_start_beats_reference_guess(cuda):
         accepted += ok
     assert accepted == len(test)
     assert np.mean(it_learned) < 0.6 * np.mean(it_plain)
+
+
+def test_slab_problem_from_converged_state(oracle):
+    """SlabProblem on the oracle: the reference path converges, and starting
+    from its converged state the full-load Newton needs no iteration."""
+    m = M.guccione_slab(3, 3, 2, lengths=(4.0, 4.0, 1.0), seed=3)
+    es = oracle.EquationsSet(m)
+    pb = W.SlabProblem(es, N.NewtonOptions(linear="dense"), device="cpu")
+    p = W.sample_slab_parameters(1, seed=4)[0]
+    x, reps, _ = pb.solve_reference(p, 4)
+    assert all(r.converged for r in reps)
+    x2, reps2, _, ok = pb.solve_from_state(p, pb.state(x), 4)
+    assert ok and reps2[0].iterations == 0
+    assert float((x2 - x).abs().max()) == 0.0
+    f = W.slab_features(W.sample_slab_parameters(5, seed=1))
+    assert f.shape == (5, 2)
+
+
+@pytest.mark.gpu
+def test_learned_warm_start_on_the_slab(cuda):
+    """Guccione slab over (cavity pressure, C): trained on plain-method solves,
+    Newton from the prediction at the full pressure needs fewer iterations
+    than the pressure-increment path, at the same ||r||_2 <= 1e-10."""
+    from cm_gb300 import FiniteElasticityEquationsSet
+    m = M.guccione_slab(3, 3, 2, lengths=(4.0, 4.0, 1.0), seed=3)
+    es = FiniteElasticityEquationsSet(m)
+    plain = W.SlabProblem(es, N.NewtonOptions(linear="dense"), device=cuda)
+    fast = W.SlabProblem(es, N.NewtonOptions(linear="dense", precision="mixed"), device=cuda)
+    train = W.sample_slab_parameters(64, seed=31)
+    test = W.sample_slab_parameters(6, seed=32)
+    states, _ = W.generate_solves(plain, train, 4)
+    ws = W.LearnedWarmStart(plain.n_pressure, modes=24, hidden=(128, 128, 128), seed=0, device=cuda,
+                            featurize=W.slab_features)
+    ws.fit(train, states, steps=1500, lr=2e-3, batch=64)
+    guess = ws.predict(test)
+    it_plain, it_learned = [], []
+    for p, g in zip(test, guess):
+        xr, rr, _ = plain.solve_reference(p, 4)
+        xl, rl, _, ok = fast.solve_from_state(p, g, 4)
+        assert ok and rl[-1].converged and rl[-1].residual_norms[-1] <= 1e-10
+        assert float((xl - xr).abs().max()) < 1e-8
+        it_plain.append(sum(r.iterations for r in rr))
+        it_learned.append(sum(r.iterations for r in rl))
+    assert np.mean(it_learned) < 0.6 * np.mean(it_plain)
