@@ -415,7 +415,7 @@ def our_arm(args):
         dist.destroy_process_group()
 
 
-def slab_newton_leg(dev, ex=16, ey=16, ez=4, increments=8, n_train=48, n_test=4):
+def slab_newton_leg(dev, ex=16, ey=16, ez=4, increments=8, n_train=48, n_test=4, modes=16, train_steps=4000):
     """Newton with the reference's pressure-increment rule on a Guccione slab
     (the slab configuration at reduced resolution: 40x40x10 mm, fibres -60..+60
     degrees through the thickness, lateral faces clamped, cavity pressure on
@@ -439,9 +439,9 @@ def slab_newton_leg(dev, ex=16, ey=16, ez=4, increments=8, n_train=48, n_test=4)
     t0 = time.perf_counter()
     states, it_train = W.generate_solves(fast, train, increments)
     t_data = time.perf_counter() - t0
-    ws = W.LearnedWarmStart(fast.n_pressure, modes=min(64, n_train - 1), seed=0, device=dev,
+    ws = W.LearnedWarmStart(fast.n_pressure, modes=min(modes, n_train - 1), seed=0, device=dev,
                             featurize=W.slab_features)
-    rep = ws.fit(train, states, steps=2000, lr=2e-3, batch=min(256, n_train))
+    rep = ws.fit(train, states, steps=train_steps, lr=2e-3, batch=min(256, n_train))
     plain.solve_reference(test[0], increments)      # warm-up of both paths
     fast.solve_from_state(test[0], ws.predict(test[:1])[0], increments)
     rows = []
@@ -455,6 +455,7 @@ def slab_newton_leg(dev, ex=16, ey=16, ez=4, increments=8, n_train=48, n_test=4)
         rows.append({"plain_iters": sum(r.iterations for r in rp), "plain_krylov": sum(sum(r.linear_iterations) for r in rp),
                      "plain_s": tp, "learned_iters": sum(r.iterations for r in rl),
                      "learned_krylov": sum(sum(r.linear_iterations) for r in rl), "learned_s": tl, "accepted": bool(ok),
+                     "learned_first_residual": rl[0].residual_norms[0], "plain_first_residual": rp[0].residual_norms[0],
                      "converged": bool(rp[-1].converged and rl[-1].converged),
                      "final_residual": max(rp[-1].residual_norms[-1], rl[-1].residual_norms[-1]),
                      "max_diff": float((xl - xp).abs().max()), "max_uz": float(uz.max())})
@@ -468,7 +469,8 @@ def slab_newton_leg(dev, ex=16, ey=16, ez=4, increments=8, n_train=48, n_test=4)
                        "increments": increments, "guess": "reference (current field)"},
         "mixed_learned": {"newton_iterations": mean("learned_iters"), "krylov_iterations": mean("learned_krylov"),
                           "solve_ms": 1e3 * mean("learned_s"), "load_step_ms": 1e3 * mean("learned_s"),
-                          "increments": 1, "accepted_guesses": int(sum(r["accepted"] for r in rows))},
+                          "increments": 1, "accepted_guesses": int(sum(r["accepted"] for r in rows)),
+                          "initial_residuals": [r["learned_first_residual"] for r in rows]},
         "solve_speedup": mean("plain_s") / mean("learned_s"),
         "all_converged_1e-10": all(r["converged"] and r["final_residual"] <= 1e-10 for r in rows),
         "max_solution_difference": max(r["max_diff"] for r in rows),
