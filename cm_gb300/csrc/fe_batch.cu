@@ -12,11 +12,16 @@
 // one fe_jacobian_evaluate_mixed call per member to the rounding of the
 // separately compiled device code.
 //
+// Members with a surface-pressure load get, after the volume work of each
+// colour and a grid barrier, that colour's boundary elements (one warp each)
+// and a second barrier, the order of the single-set path.
+//
 // The grid barrier spins with a bounded number of polls: if it ever gives up
 // (which only a non-co-resident grid could cause, and the cooperative launch
 // rules that out), it sets bit 1 of the batch status word and the host call
 // reports an error instead of hanging.
 #include "fe_mixed_impl.cuh"
+#include "fe_surface_impl.cuh"
 
 #include <cooperative_groups.h>
 
@@ -57,8 +62,9 @@ __device__ void grid_barrier(const BatchArgs& A) {
 template <int EGQ, int EGL>
 struct BatchCfg {
   static constexpr int s(int a, int b) { return a > b ? a : b; }
-  static constexpr int WORK = s(s(MixCfg<2, 0, EGL>::SMEM, MixCfg<2, 1, EGL>::SMEM),
-                                s(MixCfg<3, 0, EGQ>::SMEM, MixCfg<3, 1, EGQ>::SMEM));
+  static constexpr int WORK = s(s(s(MixCfg<2, 0, EGL>::SMEM, MixCfg<2, 1, EGL>::SMEM),
+                                  s(MixCfg<3, 0, EGQ>::SMEM, MixCfg<3, 1, EGQ>::SMEM)),
+                                (int)(BT_THREADS / 32 * sizeof(SurfWarpSmem)));
   static constexpr int O_WORK = align16((int)sizeof(KParams));
   static constexpr int SMEM = O_WORK + WORK;
 };
@@ -118,6 +124,39 @@ __global__ void __launch_bounds__(BT_THREADS, MINB) fe_mixed_batch_kernel(BatchA
       for (int g = it.y; g < it.y + it.z; ++g) run_group<EGQ, EGL, H>(it.w, *kp, g, p4_first, work);
     }
     grid_barrier(A);
+    if (A.sitem_ptr[c + 1] > A.sitem_ptr[c]) {  // surface loads of this colour (grid-uniform test)
+      SurfWarpSmem* ws = reinterpret_cast<SurfWarpSmem*>(work);
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int w = A.sitem_ptr[c] + blockIdx.x; w < A.sitem_ptr[c + 1]; w += gridDim.x) {
+        const int4 it = reinterpret_cast<const int4*>(A.sitems)[w];
+        __syncthreads();
+        if (it.x != cur_kp) {
+          const uint32_t* src = reinterpret_cast<const uint32_t*>(&A.kps[it.x]);
+          uint32_t* dst = reinterpret_cast<uint32_t*>(kp);
+          for (int i = threadIdx.x; i < (int)(sizeof(KParams) / 4); i += blockDim.x) dst[i] = src[i];
+          __syncthreads();
+          if (threadIdx.x == 0) {
+            const BatchPtrs p = A.ptrs[it.x / A.ncol_kp];
+            kp->x = p.x;
+            kp->r = p.r;
+            kp->vals = p.vals;
+            kp->vals_uu = p.vals_uu;
+          }
+          __syncthreads();
+          cur_kp = it.x;
+        }
+        const cmfe::BatchSurf sf = A.surf[it.x / A.ncol_kp];
+        if (warp < it.z) {
+          const int e = sf.belems[it.y + warp];
+          if (it.w == 3)
+            surface_element<3>(*kp, e, sf.bmask, 0, 1, ws[warp], lane);
+          else
+            surface_element<2>(*kp, e, sf.bmask, 0, 1, ws[warp], lane);
+        }
+      }
+      cur_type = -1;  // the constant tables were overwritten
+      grid_barrier(A);
+    }
   }
 }
 

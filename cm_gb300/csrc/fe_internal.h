@@ -115,11 +115,19 @@ struct BatchPtrs {
   float* vals_uu;
 };
 
+struct BatchSurf {
+  const int32_t* belems;     // boundary elements of the member, grouped by colour
+  const uint8_t* bmask;      // boundary faces per element
+};
+
 struct BatchArgs {
   const KParams* kps;        // [member][colour]
   const BatchPtrs* ptrs;     // [member]
   const int32_t* items;      // 4 ints per work item: kp index, first group, groups, element type
   const int32_t* item_ptr;   // [colour + 1]
+  const int32_t* sitems;     // surface-pressure items: kp index, first boundary element, count (<= 8), n1
+  const int32_t* sitem_ptr;  // [colour + 1]
+  const BatchSurf* surf;     // [member]
   int ncolours;
   int ncol_kp;               // colours per member in kps
   unsigned* bar_count;       // grid barrier state (zero before a launch)

@@ -498,6 +498,10 @@ struct fe_batch_s {
   cmfe::BatchPtrs* h_ptrs = nullptr;  // pinned copy of the last uploaded table
   int32_t* d_items = nullptr;
   int32_t* d_item_ptr = nullptr;
+  int32_t* d_sitems = nullptr;      // surface-pressure work items
+  int32_t* d_sitem_ptr = nullptr;
+  cmfe::BatchSurf* d_surf = nullptr;
+  std::vector<const void*> surf_sig;  // per member: d_surfp when loaded, else NULL
   unsigned* d_sync = nullptr;      // [0] barrier count, [1] barrier generation, [2] status
   int variant = 1, ctas_per_sm = 2, block_groups = 1;
   int items_variant = -1, items_block = -1;
@@ -716,9 +720,55 @@ int batch_set_pointers(fe_batch b, const double* const* x, float* const* uu, dou
   return FE_NO_ERROR;
 }
 
+// Surface-pressure state of the members: when it changed since the last
+// call, the members' parameters (pressure pointer) and the surface work items
+// (boundary elements of each colour, up to 8 per item, one warp each) are
+// rebuilt.
+int refresh_surface(fe_batch b) {
+  const size_t n = b->members.size();
+  std::vector<const void*> sig(n);
+  for (size_t m = 0; m < n; ++m) sig[m] = b->members[m]->has_surfp ? (const void*)b->members[m]->d_surfp : nullptr;
+  if (sig == b->surf_sig && b->d_sitem_ptr) return FE_NO_ERROR;
+  std::vector<int32_t> items, ptr(1, 0);
+  std::vector<cmfe::BatchSurf> surf(n);
+  for (size_t m = 0; m < n; ++m) {
+    fe_handle h = b->members[m];
+    surf[m] = {h->d_bnd_elems, h->d_bnd_mask};
+    for (int c = 0; c < b->ncol; ++c) b->kps[m * b->ncol + c].surf_p = h->d_surfp;
+  }
+  for (int c = 0; c < b->ncol; ++c) {
+    for (size_t m = 0; m < n; ++m) {
+      fe_handle h = b->members[m];
+      if (!sig[m] || c >= h->hs.ncolours) continue;
+      const int first = h->hs.bnd_ptr[c], nb = h->hs.bnd_ptr[c + 1] - first;
+      for (int j = 0; j < nb; j += 8) {
+        items.push_back((int32_t)(m * b->ncol + c));
+        items.push_back(first + j);
+        items.push_back(std::min(8, nb - j));
+        items.push_back(h->hs.n1);
+      }
+    }
+    ptr.push_back((int32_t)(items.size() / 4));
+  }
+  CUDA_TRY(cudaMemcpy(b->d_kps, b->kps.data(), b->kps.size() * sizeof(KParams), cudaMemcpyHostToDevice));
+  if (b->d_sitems) cudaFree(b->d_sitems);
+  b->d_sitems = nullptr;
+  if (!items.empty()) {
+    CUDA_TRY(cudaMalloc(&b->d_sitems, items.size() * sizeof(int32_t)));
+    CUDA_TRY(cudaMemcpy(b->d_sitems, items.data(), items.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  }
+  if (!b->d_sitem_ptr) CUDA_TRY(cudaMalloc(&b->d_sitem_ptr, ptr.size() * sizeof(int32_t)));
+  CUDA_TRY(cudaMemcpy(b->d_sitem_ptr, ptr.data(), ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  if (!b->d_surf) CUDA_TRY(cudaMalloc(&b->d_surf, n * sizeof(cmfe::BatchSurf)));
+  CUDA_TRY(cudaMemcpy(b->d_surf, surf.data(), n * sizeof(cmfe::BatchSurf), cudaMemcpyHostToDevice));
+  b->surf_sig = sig;
+  return FE_NO_ERROR;
+}
+
 int batch_launch(fe_batch b, cudaStream_t st) {
   int rc = build_items(b, b->variant, b->block_groups);
   if (rc) return rc;
+  if ((rc = refresh_surface(b))) return rc;
   CUDA_TRY(cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned), st));
   cmfe::BatchArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -726,6 +776,9 @@ int batch_launch(fe_batch b, cudaStream_t st) {
   a.ptrs = b->d_ptrs;
   a.items = b->d_items;
   a.item_ptr = b->d_item_ptr;
+  a.sitems = b->d_sitems;
+  a.sitem_ptr = b->d_sitem_ptr;
+  a.surf = b->d_surf;
   a.ncolours = b->ncol;
   a.ncol_kp = b->ncol;
   a.bar_count = b->d_sync;
@@ -1192,7 +1245,7 @@ int fe_batch_destroy(fe_batch b) {
   if (!b) return FE_NO_ERROR;
   if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
   if (b->graph) cudaGraphDestroy(b->graph);
-  void* ptrs[] = {b->d_kps, b->d_ptrs, b->d_items, b->d_item_ptr, b->d_sync};
+  void* ptrs[] = {b->d_kps, b->d_ptrs, b->d_items, b->d_item_ptr, b->d_sync, b->d_sitems, b->d_sitem_ptr, b->d_surf};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->h_ptrs) cudaFreeHost(b->h_ptrs);
@@ -1206,8 +1259,6 @@ int fe_batch_jacobian_evaluate_mixed(fe_batch b, const double* const* x, float* 
   if (rc) return rc;
   if (!x || !values_uu || !values_coupling) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL pointer array");
   std::lock_guard<std::mutex> lk(b->mu);
-  for (fe_handle h : b->members)
-    if (h->has_surfp) return set_error(FE_ERR_NOT_SUPPORTED, "batched evaluation of a member with surface pressure");
   cudaStream_t st = (cudaStream_t)stream;
   if ((rc = batch_set_pointers(b, x, values_uu, values_coupling, r, st))) return rc;
   return batch_launch(b, st);
@@ -1313,6 +1364,7 @@ int fe_batch_capture(fe_batch b, const double* const* x, float* const* values_uu
   cudaStream_t st = (cudaStream_t)stream;
   if ((rc = batch_set_pointers(b, x, values_uu, values_coupling, r, st))) return rc;
   if ((rc = build_items(b, b->variant, b->block_groups))) return rc;
+  if ((rc = refresh_surface(b))) return rc;
   cudaStream_t cs;
   CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);

@@ -189,8 +189,10 @@ int fe_element_jacobians(fe_handle h, const double* x, int32_t first, int32_t co
  * with a grid barrier between colours.  Repeated launches are bit-identical;
  * the result agrees with one fe_jacobian_evaluate_mixed call per member to
  * FP32 rounding in the displacement block and FP64 rounding elsewhere.  The
- * member handles must outlive the batch; members with surface pressure are
- * not supported; the residual and coupling blocks are computed in FP64. */
+ * member handles must outlive the batch; members with a surface-pressure
+ * load get their boundary faces after each colour's volume work (a second
+ * grid barrier per colour); the residual and coupling blocks are computed in
+ * FP64. */
 typedef struct fe_batch_s* fe_batch;
 
 int fe_batch_create(const fe_handle* handles, int32_t count, fe_batch* out);
@@ -218,7 +220,8 @@ int fe_batch_autotune(fe_batch b, const double* const* x, float* const* values_u
                       double* const* values_coupling, double* const* r, int32_t repeats, void* stream);
 
 /* Captures one batched assembly with the given buffers into a CUDA graph;
- * fe_batch_replay() launches it on stream (same buffers, current inputs). */
+ * fe_batch_replay() launches it on stream (same buffers, current inputs; the
+ * members' surface-pressure loads as they were at capture). */
 int fe_batch_capture(fe_batch b, const double* const* x, float* const* values_uu,
                      double* const* values_coupling, double* const* r, void* stream);
 int fe_batch_replay(fe_batch b, void* stream);

@@ -108,3 +108,42 @@ def test_batch_rejects_host_pointers(torch):
     xs_host = [x.cpu() for x in xs]
     with pytest.raises(FEError):
         batch.jacobian_evaluate_mixed(xs_host, vus, vcs, rs)
+
+
+def test_batch_with_surface_pressure(torch):
+    """Members carrying a follower surface-pressure load (and members without
+    one) in one batch: agrees with the single-set mixed evaluation, which
+    applies each colour's boundary faces after its volume work."""
+    from cm_gb300 import EquationsSetBatch, FiniteElasticityEquationsSet
+    ms = [M.guccione_slab(3, 3, 2, lengths=(4.0, 4.0, 1.0), seed=3),
+          M.regular_box(3, 2, 2, nxi_u=2, pressure="element", law=M.MR, materials=(2.0, 6.0), perturb=0.05, seed=4),
+          M.regular_box(2, 2, 2, nxi_u=3, pressure="node", law=M.MR, materials=(1.0, 4.0))]
+    sets = [FiniteElasticityEquationsSet(m) for m in ms]
+    for m, s in zip(ms[:2], sets[:2]):
+        sp = np.zeros((3, m.nu))
+        i, j, k = m.node_ijk()
+        sp[2, k == 0] = 1.5
+        sp[0, i == i.max()] = -0.3
+        s.set_surface_pressure(sp)
+    xs = [torch.from_numpy(M.deformed_state(m, stretch=1.04, shear=0.02, noise=0.02, seed=i + 7)).cuda()
+          for i, m in enumerate(ms)]
+    refs = []
+    for s, x in zip(sets, xs):
+        r = torch.empty_like(x)
+        vu, vc = s.jacobian_evaluate_mixed(x, r=r)
+        s.check_status(x)
+        refs.append((vu.clone(), vc.clone(), r.clone()))
+    batch = EquationsSetBatch(sets)
+    vus, vcs, rs = batch.allocate("cuda")
+    for variant in (1, 4):
+        batch.set_config(variant, 2, 1)
+        batch.jacobian_evaluate_mixed(xs, vus, vcs, rs)
+        batch.check(xs[0])
+        _close(torch, refs, vus, vcs, rs)
+    # removing the load from a member is seen by the next batched call
+    sets[0].set_surface_pressure(None)
+    r0 = torch.empty_like(xs[0])
+    vu0, vc0 = sets[0].jacobian_evaluate_mixed(xs[0], r=r0)
+    batch.jacobian_evaluate_mixed(xs, vus, vcs, rs)
+    batch.check(xs[0])
+    _close(torch, [(vu0, vc0, r0)], vus[:1], vcs[:1], rs[:1])
