@@ -106,42 +106,46 @@ int launch_surface(const HostSetup& s, const KParams& kp, const int32_t* belems,
 // Builds the set-up; returns FE_NO_ERROR or a FE_ERR_* code with msg filled.
 int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg);
 
-// Batched mixed assembly (fe_batch.cu): per-member output pointers and the
-// arguments of the persistent launch.
-struct BatchPtrs {
-  const double* x;
-  double* r;
-  double* vals;
-  float* vals_uu;
-};
+// Batched mixed assembly (fe_batch.cu).  The members' parameters live in a
+// constant-memory table of the batch module, one entry per member slot
+// (slots ordered by element type), so that the persistent kernel reads them
+// as warp-uniform operands, as the single-set kernels read their launch
+// parameters.
+constexpr int BATCH_MAX_MEMBERS = 256;
 
-struct BatchSurf {
-  const int32_t* belems;     // boundary elements of the member, grouped by colour
+struct BatchMember {
+  KParams kp;                // elems: the member's colour-ordered element list; x, r, vals, vals_uu of the call
+  const int32_t* belems;     // boundary elements grouped by colour
   const uint8_t* bmask;      // boundary faces per element
+  int type;                  // 2 * (N1 == 3) + nodal pressure
+  int has_surface;           // surface-pressure load set (kp.surf_p)
 };
 
 struct BatchArgs {
-  const KParams* kps;        // [member][colour]
-  const BatchPtrs* ptrs;     // [member]
-  const int32_t* items;      // 4 ints per work item: kp index, first group, groups, element type
-  const int32_t* item_ptr;   // [colour + 1]
-  const int32_t* sitems;     // surface-pressure items: kp index, first boundary element, count (<= 8), n1
-  const int32_t* sitem_ptr;  // [colour + 1]
-  const BatchSurf* surf;     // [member]
+  const int32_t* offsets;    // [slot][2][ncolours + 1]: colour element offsets, then boundary element offsets
+  int nmembers;
   int ncolours;
-  int ncol_kp;               // colours per member in kps
+  int block_groups;          // consecutive element groups per work unit
+  int wave;                  // CTAs per launch wave (the SM count)
   unsigned* bar_count;       // grid barrier state (zero before a launch)
   unsigned* bar_gen;
   unsigned* status;          // bit 1: a grid barrier gave up waiting
-  int wave;
 };
 
 // Number of launch variants, their elements per group (triquadratic,
-// trilinear) and dynamic shared memory; the launch returns a cudaError_t.
+// trilinear) and dynamic shared memory for the element types present (mask
+// bit t = type t, bit 4 = surface loads).
 int batch_variants();
 int batch_variant_eg(int v, int* egq, int* egl);
-int batch_smem(int v);
-int launch_mixed_batch(int variant, const BatchArgs& a, int ctas_per_sm, int num_sms, void* stream);
+int batch_smem(int v, unsigned mask);
+// Copies the member table (device memory, n entries) into the constant table
+// and launches the persistent kernel, both on stream; returns a cudaError_t.
+int launch_mixed_batch(int variant, unsigned mask, const BatchMember* members, int n, const BatchArgs& a,
+                       int ctas_per_sm, int num_sms, void* stream);
+// The same for a batch whose members all have element type `type`
+// (fe_batch_typed.cu).
+int launch_batch_typed(int variant, int type, unsigned mask, const BatchMember* members, int n, const BatchArgs& a,
+                       int ctas_per_sm, int num_sms, void* stream);
 
 // Records the text fe_last_error() returns (per calling thread) and returns code.
 int record_error(int code, const std::string& msg);

@@ -491,21 +491,17 @@ struct fe_batch_s {
   std::vector<fe_handle> members;
   int device = 0;
   int num_sms = 0;
-  int ncol = 0;                    // colours per member slot in kps
-  std::vector<KParams> kps;        // [member][colour] (output pointers set per call)
-  KParams* d_kps = nullptr;
-  cmfe::BatchPtrs* d_ptrs = nullptr;
-  cmfe::BatchPtrs* h_ptrs = nullptr;  // pinned copy of the last uploaded table
-  int32_t* d_items = nullptr;
-  int32_t* d_item_ptr = nullptr;
-  int32_t* d_sitems = nullptr;      // surface-pressure work items
-  int32_t* d_sitem_ptr = nullptr;
-  cmfe::BatchSurf* d_surf = nullptr;
+  int ncol = 0;                       // colours: the most of any member
+  std::vector<int32_t> slot_member;   // member of each constant-table slot (slots ordered by element type)
+  cmfe::BatchMember* h_table = nullptr;   // pinned host copy of the member table
+  cmfe::BatchMember* d_table = nullptr;   // device copy, source of the constant table for direct launches
+  cmfe::BatchMember* d_table_graph = nullptr;  // snapshot taken at capture, source for graph replays
+  bool table_dirty = true;
+  int32_t* d_offsets = nullptr;       // [slot][2][ncol + 1]: colour element offsets, boundary element offsets
   std::vector<const void*> surf_sig;  // per member: d_surfp when loaded, else NULL
-  unsigned* d_sync = nullptr;      // [0] barrier count, [1] barrier generation, [2] status
+  unsigned* d_sync = nullptr;         // [0] barrier count, [1] barrier generation, [2] status
   int variant = 1, ctas_per_sm = 2, block_groups = 1;
-  int items_variant = -1, items_block = -1;
-  int64_t nitems = 0;
+  unsigned type_mask = 0;             // element types present (bit 4: surface loads)
   double tuned_ms = -1.0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -661,134 +657,108 @@ namespace {
 
 int member_type(const HostSetup& s) { return (s.n1 == 3 ? 2 : 0) + (s.pmode ? 1 : 0); }
 
-// Work items of every colour for a launch variant: (kp index, first group,
-// groups, element type), element types contiguous within a colour.
-int build_items(fe_batch b, int variant, int block_groups) {
-  if (b->items_variant == variant && b->items_block == block_groups) return FE_NO_ERROR;
-  int egq = 0, egl = 0;
-  if (cmfe::batch_variant_eg(variant, &egq, &egl)) return set_error(FE_ERR_INVALID_ARGUMENT, "unknown batch variant");
-  std::vector<int32_t> items, ptr(1, 0);
-  for (int c = 0; c < b->ncol; ++c) {
-    for (int t = 0; t < 4; ++t)
-      for (size_t m = 0; m < b->members.size(); ++m) {
-        const HostSetup& hs = b->members[m]->hs;
-        if (member_type(hs) != t || c >= hs.ncolours) continue;
-        const int count = hs.colour_ptr[c + 1] - hs.colour_ptr[c];
-        const int eg = hs.n1 == 3 ? egq : egl;
-        const int groups = (count + eg - 1) / eg;
-        for (int g = 0; g < groups; g += block_groups) {
-          items.push_back((int32_t)(m * b->ncol + c));
-          items.push_back(g);
-          items.push_back(std::min(block_groups, groups - g));
-          items.push_back(t);
-        }
-      }
-    ptr.push_back((int32_t)(items.size() / 4));
-  }
-  if (b->d_items) cudaFree(b->d_items);
-  b->d_items = nullptr;
-  if (!items.empty()) CUDA_TRY(cudaMalloc(&b->d_items, items.size() * sizeof(int32_t)));
-  if (!items.empty())
-    CUDA_TRY(cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(b->d_item_ptr, ptr.data(), ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-  b->items_variant = variant;
-  b->items_block = block_groups;
-  b->nitems = (int64_t)items.size() / 4;
+// The batched kernel reads the member table from the batch module's constant
+// memory: launches of all batches on a device are serialised through one
+// event per device, so that no launch overwrites the table while another
+// batch's kernel still reads it.
+std::mutex g_batch_mu;
+cudaEvent_t g_batch_event[64] = {};
+
+int batch_serialise_begin(int device, cudaStream_t st) {
+  if (device < 0 || device >= 64) return set_error(FE_ERR_NOT_SUPPORTED, "device ordinal out of range");
+  if (!g_batch_event[device]) CUDA_TRY(cudaEventCreateWithFlags(&g_batch_event[device], cudaEventDisableTiming));
+  CUDA_TRY(cudaStreamWaitEvent(st, g_batch_event[device], 0));
   return FE_NO_ERROR;
 }
 
-// Uploads the per-member output pointers when they changed since the last call.
+int batch_serialise_end(int device, cudaStream_t st) {
+  CUDA_TRY(cudaEventRecord(g_batch_event[device], st));
+  return FE_NO_ERROR;
+}
+
+// Sets the per-call output pointers of every slot (uploaded with the table).
 int batch_set_pointers(fe_batch b, const double* const* x, float* const* uu, double* const* cp, double* const* r,
                        cudaStream_t st) {
+  (void)st;
   const size_t n = b->members.size();
-  bool changed = false;
   for (size_t m = 0; m < n; ++m) {
     if (!x[m] || !uu[m] || !cp[m]) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL member pointer");
     if (!is_device_ptr(x[m]) || !is_device_ptr(uu[m]) || !is_device_ptr(cp[m]) || (r && r[m] && !is_device_ptr(r[m])))
       return set_error(FE_ERR_INVALID_ARGUMENT, "batched evaluation takes device pointers only");
-    cmfe::BatchPtrs p{x[m], r ? r[m] : nullptr, cp[m], uu[m]};
-    if (std::memcmp(&p, &b->h_ptrs[m], sizeof(p)) != 0) {
-      b->h_ptrs[m] = p;
-      changed = true;
-    }
   }
-  if (changed) {
-    // the pinned table is rewritten by the next call: wait for this copy
-    CUDA_TRY(cudaMemcpyAsync(b->d_ptrs, b->h_ptrs, n * sizeof(cmfe::BatchPtrs), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
+  for (size_t s = 0; s < n; ++s) {
+    const int m = b->slot_member[s];
+    KParams& k = b->h_table[s].kp;
+    double* rr = r ? r[m] : nullptr;
+    if (k.x != x[m] || k.r != rr || k.vals != cp[m] || k.vals_uu != uu[m]) {
+      k.x = x[m];
+      k.r = rr;
+      k.vals = cp[m];
+      k.vals_uu = uu[m];
+      b->table_dirty = true;
+    }
   }
   return FE_NO_ERROR;
 }
 
-// Surface-pressure state of the members: when it changed since the last
-// call, the members' parameters (pressure pointer) and the surface work items
-// (boundary elements of each colour, up to 8 per item, one warp each) are
-// rebuilt.
+// Surface-pressure state of the members (pressure pointer per slot).
 int refresh_surface(fe_batch b) {
   const size_t n = b->members.size();
   std::vector<const void*> sig(n);
   for (size_t m = 0; m < n; ++m) sig[m] = b->members[m]->has_surfp ? (const void*)b->members[m]->d_surfp : nullptr;
-  if (sig == b->surf_sig && b->d_sitem_ptr) return FE_NO_ERROR;
-  std::vector<int32_t> items, ptr(1, 0);
-  std::vector<cmfe::BatchSurf> surf(n);
-  for (size_t m = 0; m < n; ++m) {
-    fe_handle h = b->members[m];
-    surf[m] = {h->d_bnd_elems, h->d_bnd_mask};
-    for (int c = 0; c < b->ncol; ++c) b->kps[m * b->ncol + c].surf_p = h->d_surfp;
+  if (sig == b->surf_sig) return FE_NO_ERROR;
+  bool any = false;
+  for (size_t s = 0; s < n; ++s) {
+    const int m = b->slot_member[s];
+    b->h_table[s].kp.surf_p = static_cast<const double*>(sig[m]);
+    b->h_table[s].has_surface = sig[m] != nullptr;
+    any = any || sig[m] != nullptr;
   }
-  for (int c = 0; c < b->ncol; ++c) {
-    for (size_t m = 0; m < n; ++m) {
-      fe_handle h = b->members[m];
-      if (!sig[m] || c >= h->hs.ncolours) continue;
-      const int first = h->hs.bnd_ptr[c], nb = h->hs.bnd_ptr[c + 1] - first;
-      for (int j = 0; j < nb; j += 8) {
-        items.push_back((int32_t)(m * b->ncol + c));
-        items.push_back(first + j);
-        items.push_back(std::min(8, nb - j));
-        items.push_back(h->hs.n1);
-      }
-    }
-    ptr.push_back((int32_t)(items.size() / 4));
-  }
-  CUDA_TRY(cudaMemcpy(b->d_kps, b->kps.data(), b->kps.size() * sizeof(KParams), cudaMemcpyHostToDevice));
-  if (b->d_sitems) cudaFree(b->d_sitems);
-  b->d_sitems = nullptr;
-  if (!items.empty()) {
-    CUDA_TRY(cudaMalloc(&b->d_sitems, items.size() * sizeof(int32_t)));
-    CUDA_TRY(cudaMemcpy(b->d_sitems, items.data(), items.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-  }
-  if (!b->d_sitem_ptr) CUDA_TRY(cudaMalloc(&b->d_sitem_ptr, ptr.size() * sizeof(int32_t)));
-  CUDA_TRY(cudaMemcpy(b->d_sitem_ptr, ptr.data(), ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-  if (!b->d_surf) CUDA_TRY(cudaMalloc(&b->d_surf, n * sizeof(cmfe::BatchSurf)));
-  CUDA_TRY(cudaMemcpy(b->d_surf, surf.data(), n * sizeof(cmfe::BatchSurf), cudaMemcpyHostToDevice));
+  b->type_mask = any ? (b->type_mask | 16u) : (b->type_mask & 15u);
   b->surf_sig = sig;
+  b->table_dirty = true;
+  return FE_NO_ERROR;
+}
+
+// Uploads the host member table to its device copy when it changed.
+int sync_table(fe_batch b, cudaStream_t st) {
+  if (!b->table_dirty) return FE_NO_ERROR;
+  const size_t bytes = b->members.size() * sizeof(cmfe::BatchMember);
+  // the pinned table is rewritten by a later call: wait for this copy
+  CUDA_TRY(cudaMemcpyAsync(b->d_table, b->h_table, bytes, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  b->table_dirty = false;
+  return FE_NO_ERROR;
+}
+
+// One batched launch on st; table is the device copy of the member table the
+// launch copies into constant memory.
+int batch_launch_from(fe_batch b, const cmfe::BatchMember* table, cudaStream_t st) {
+  CUDA_TRY(cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned), st));
+  cmfe::BatchArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.offsets = b->d_offsets;
+  a.nmembers = (int)b->members.size();
+  a.ncolours = b->ncol;
+  a.block_groups = b->block_groups;
+  a.bar_count = b->d_sync;
+  a.bar_gen = b->d_sync + 1;
+  a.status = b->d_sync + 2;
+  const int e = cmfe::launch_mixed_batch(b->variant, b->type_mask, table, (int)b->members.size(), a, b->ctas_per_sm,
+                                         b->num_sms, st);
+  if (e != 0) return set_error(FE_ERR_CUDA, std::string("batched kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+  b->launches++;
   return FE_NO_ERROR;
 }
 
 int batch_launch(fe_batch b, cudaStream_t st) {
-  int rc = build_items(b, b->variant, b->block_groups);
-  if (rc) return rc;
-  if ((rc = refresh_surface(b))) return rc;
-  CUDA_TRY(cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned), st));
-  cmfe::BatchArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.kps = b->d_kps;
-  a.ptrs = b->d_ptrs;
-  a.items = b->d_items;
-  a.item_ptr = b->d_item_ptr;
-  a.sitems = b->d_sitems;
-  a.sitem_ptr = b->d_sitem_ptr;
-  a.surf = b->d_surf;
-  a.ncolours = b->ncol;
-  a.ncol_kp = b->ncol;
-  a.bar_count = b->d_sync;
-  a.bar_gen = b->d_sync + 1;
-  a.status = b->d_sync + 2;
-  if (b->nitems == 0) return FE_NO_ERROR;
-  const int e = cmfe::launch_mixed_batch(b->variant, a, b->ctas_per_sm, b->num_sms, st);
-  if (e != 0) return set_error(FE_ERR_CUDA, std::string("batched kernel launch: ") + cudaGetErrorString((cudaError_t)e));
-  b->launches++;
-  return FE_NO_ERROR;
+  int rc = refresh_surface(b);
+  if (rc || (rc = sync_table(b, st))) return rc;
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  if ((rc = batch_serialise_begin(b->device, st))) return rc;
+  rc = batch_launch_from(b, b->d_table, st);
+  const int rc2 = batch_serialise_end(b->device, st);
+  return rc ? rc : rc2;
 }
 
 int check_batch(fe_batch b) {
@@ -1207,29 +1177,45 @@ int fe_batch_create(const fe_handle* handles, int32_t count, fe_batch* out) {
       b->ncol = std::max(b->ncol, handles[i]->hs.ncolours);
     }
   }
+  if (!rc && count > cmfe::BATCH_MAX_MEMBERS)
+    rc = set_error(FE_ERR_NOT_SUPPORTED, "a batch holds at most " + std::to_string(cmfe::BATCH_MAX_MEMBERS) + " members");
   if (!rc) {
     b->num_sms = b->members[0]->num_sms;
-    b->kps.resize((size_t)count * b->ncol);
-    for (int32_t m = 0; m < count; ++m) {
-      fe_handle h = b->members[m];
-      for (int c = 0; c < b->ncol; ++c) {
-        KParams k = base_params(h);
-        if (c < h->hs.ncolours) {
-          k.elems = h->d_colour_elems + h->hs.colour_ptr[c];
-          k.count = h->hs.colour_ptr[c + 1] - h->hs.colour_ptr[c];
-        }
-        b->kps[(size_t)m * b->ncol + c] = k;
-      }
-    }
+    // slots ordered by element type, members in their given order within a type
+    for (int t = 0; t < 4; ++t)
+      for (int32_t m = 0; m < count; ++m)
+        if (member_type(b->members[m]->hs) == t) b->slot_member.push_back(m);
     auto fail = [&](cudaError_t e) {
       return e == cudaSuccess ? FE_NO_ERROR : set_error(FE_ERR_CUDA, std::string("batch set-up: ") + cudaGetErrorString(e));
     };
-    rc = fail(cudaMalloc(&b->d_kps, b->kps.size() * sizeof(KParams)));
-    if (!rc) rc = fail(cudaMemcpy(b->d_kps, b->kps.data(), b->kps.size() * sizeof(KParams), cudaMemcpyHostToDevice));
-    if (!rc) rc = fail(cudaMalloc(&b->d_ptrs, (size_t)count * sizeof(cmfe::BatchPtrs)));
-    if (!rc) rc = fail(cudaMallocHost(&b->h_ptrs, (size_t)count * sizeof(cmfe::BatchPtrs)));
-    if (!rc) std::memset(b->h_ptrs, 0, (size_t)count * sizeof(cmfe::BatchPtrs));
-    if (!rc) rc = fail(cudaMalloc(&b->d_item_ptr, (size_t)(b->ncol + 1) * sizeof(int32_t)));
+    const size_t tbytes = (size_t)count * sizeof(cmfe::BatchMember);
+    rc = fail(cudaMallocHost(&b->h_table, tbytes));
+    if (!rc) rc = fail(cudaMalloc(&b->d_table, tbytes));
+    if (!rc) rc = fail(cudaMalloc(&b->d_table_graph, tbytes));
+    std::vector<int32_t> offsets((size_t)count * 2 * (b->ncol + 1));
+    for (int32_t s = 0; s < count && !rc; ++s) {
+      fe_handle h = b->members[b->slot_member[s]];
+      const HostSetup& hs = h->hs;
+      b->type_mask |= 1u << member_type(hs);
+      cmfe::BatchMember& e = b->h_table[s];
+      std::memset(&e, 0, sizeof(e));
+      e.kp = base_params(h);
+      e.kp.elems = h->d_colour_elems;
+      e.kp.count = hs.ne;
+      e.kp.surf_p = nullptr;
+      e.belems = h->d_bnd_elems;
+      e.bmask = h->d_bnd_mask;
+      e.type = member_type(hs);
+      e.has_surface = 0;
+      int32_t* o = &offsets[(size_t)s * 2 * (b->ncol + 1)];
+      for (int c = 0; c <= b->ncol; ++c) {
+        o[c] = hs.colour_ptr[std::min(c, hs.ncolours)];
+        o[b->ncol + 1 + c] = hs.bnd_ptr[std::min(c, hs.ncolours)];
+      }
+    }
+    b->surf_sig.assign((size_t)count, nullptr);
+    if (!rc) rc = fail(cudaMalloc(&b->d_offsets, offsets.size() * sizeof(int32_t)));
+    if (!rc) rc = fail(cudaMemcpy(b->d_offsets, offsets.data(), offsets.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     if (!rc) rc = fail(cudaMalloc(&b->d_sync, 4 * sizeof(unsigned)));
     if (!rc) rc = fail(cudaMemset(b->d_sync, 0, 4 * sizeof(unsigned)));
   }
@@ -1245,10 +1231,10 @@ int fe_batch_destroy(fe_batch b) {
   if (!b) return FE_NO_ERROR;
   if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
   if (b->graph) cudaGraphDestroy(b->graph);
-  void* ptrs[] = {b->d_kps, b->d_ptrs, b->d_items, b->d_item_ptr, b->d_sync, b->d_sitems, b->d_sitem_ptr, b->d_surf};
+  void* ptrs[] = {b->d_table, b->d_table_graph, b->d_offsets, b->d_sync};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  if (b->h_ptrs) cudaFreeHost(b->h_ptrs);
+  if (b->h_table) cudaFreeHost(b->h_table);
   delete b;
   return FE_NO_ERROR;
 }
@@ -1318,7 +1304,7 @@ int fe_batch_autotune(fe_batch b, const double* const* x, float* const* values_u
   for (int v = 0; v < cmfe::batch_variants() && !rc; ++v)
     for (int cps = 1; cps <= 3 && !rc; ++cps) {
       // skip a CTA count the shared memory cannot hold (the launch would use fewer)
-      if (cps * (cmfe::batch_smem(v) + 1024) > 232448) continue;
+      if (cps * (cmfe::batch_smem(v, b->type_mask) + 1024) > 232448) continue;
       for (int bg : blocks) {
         b->variant = v;
         b->ctas_per_sm = cps;
@@ -1352,7 +1338,7 @@ int fe_batch_autotune(fe_batch b, const double* const* x, float* const* values_u
   b->ctas_per_sm = bc;
   b->block_groups = bb;
   b->tuned_ms = best;
-  return build_items(b, bv, bb);
+  return FE_NO_ERROR;
 }
 
 int fe_batch_capture(fe_batch b, const double* const* x, float* const* values_uu, double* const* values_coupling,
@@ -1363,8 +1349,17 @@ int fe_batch_capture(fe_batch b, const double* const* x, float* const* values_uu
   std::lock_guard<std::mutex> lk(b->mu);
   cudaStream_t st = (cudaStream_t)stream;
   if ((rc = batch_set_pointers(b, x, values_uu, values_coupling, r, st))) return rc;
-  if ((rc = build_items(b, b->variant, b->block_groups))) return rc;
-  if ((rc = refresh_surface(b))) return rc;
+  if ((rc = refresh_surface(b)) || (rc = sync_table(b, st))) return rc;
+  {
+    // the graph reads its own snapshot of the table, written after every
+    // launch already queued on the device (an earlier replay may read it)
+    std::lock_guard<std::mutex> g(g_batch_mu);
+    if ((rc = batch_serialise_begin(b->device, st))) return rc;
+    CUDA_TRY(cudaMemcpyAsync(b->d_table_graph, b->d_table, b->members.size() * sizeof(cmfe::BatchMember),
+                             cudaMemcpyDeviceToDevice, st));
+    if ((rc = batch_serialise_end(b->device, st))) return rc;
+  }
+  CUDA_TRY(cudaStreamSynchronize(st));
   cudaStream_t cs;
   CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
@@ -1373,7 +1368,7 @@ int fe_batch_capture(fe_batch b, const double* const* x, float* const* values_uu
   b->graph = nullptr;
   cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    rc = batch_launch(b, cs);
+    rc = batch_launch_from(b, b->d_table_graph, cs);
     e = cudaStreamEndCapture(cs, &b->graph);
     if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&b->graph_exec, b->graph, 0);
   }
@@ -1387,9 +1382,12 @@ int fe_batch_replay(fe_batch b, void* stream) {
   int rc = check_batch(b);
   if (rc) return rc;
   if (!b->graph_exec) return set_error(FE_ERR_INVALID_ARGUMENT, "no captured graph: call fe_batch_capture first");
-  CUDA_TRY(cudaGraphLaunch(b->graph_exec, (cudaStream_t)stream));
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> g(g_batch_mu);
+  if ((rc = batch_serialise_begin(b->device, st))) return rc;
+  CUDA_TRY(cudaGraphLaunch(b->graph_exec, st));
   b->launches++;
-  return FE_NO_ERROR;
+  return batch_serialise_end(b->device, st);
 }
 
 int fe_batch_launch_count(fe_batch b, int64_t* count) {

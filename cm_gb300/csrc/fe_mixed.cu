@@ -13,7 +13,7 @@ __global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB) fe_mixed_kernel(KPa
   mix_tables<N1, PM, C::EG, H>(P, sm);
   const int ngroups = (P.count + C::EG - 1) / C::EG;
   const bool p4_first = (blockIdx.x / P.wave) & 1;
-  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) mix_group<N1, PM, C::EG, SPLIT, H>(P, grp, p4_first, sm);
+  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) mix_group<N1, PM, C::EG, SPLIT, H>(P, P.elems, P.count, grp, p4_first, sm);
 }
 
 template <int N1, int PM, int SPLIT, class H>

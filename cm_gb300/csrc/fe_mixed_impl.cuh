@@ -270,11 +270,12 @@ __device__ __forceinline__ void mix_tables(const KParams& P, unsigned char* sm) 
   }
 }
 
-// One group of up to EG elements, P.elems[grp*EG ...] of the current colour.
-// p4_first swaps the order of the independent FP64 (P3) and tensor-core (P4)
-// stages.
+// One group of up to EG elements, elems[grp*EG ...] of the count elements
+// of the current colour.  p4_first swaps the order of the independent FP64
+// (P3) and tensor-core (P4) stages.
 template <int N1, int PM, int EG_, int SPLIT, class H>
-__device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_first, unsigned char* sm) {
+__device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems, int count, int grp, bool p4_first,
+                                          unsigned char* sm) {
   using C = MixCfg<N1, PM, EG_>;
   constexpr int NPE = C::NPE, NPP = C::NPP, NR = C::NR, NU3 = C::NU3, NROW = C::NROW, EG = C::EG;
   constexpr int KPW = C::KPW;
@@ -296,14 +297,14 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
   int* s_node = reinterpret_cast<int*>(sm + C::O_NODE);        // [el][NR+1]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nu = P.nu;
-  const int nvalid = min(EG, P.count - grp * EG);
+  const int nvalid = min(EG, count - grp * EG);
   __syncthreads();
   // ---- P0: element nodes and table ids
   for (int i = tid; i < EG * (NR + 1); i += C::THREADS) {
     const int el = i / (NR + 1), r = i % (NR + 1);
     int v = 0;
     if (el < nvalid) {
-      const int e = P.elems[grp * EG + el];
+      const int e = elems[grp * EG + el];
       if (r < NPE)
         v = P.elem_u[(size_t)e * NPE + r];
       else if (r < NR)
@@ -382,7 +383,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
   for (int t = tid; t < EG * NG; t += C::THREADS) {
     const int el = t / NG, g = t % NG;
     if (el >= nvalid) continue;
-    const int e = P.elems[grp * EG + el];
+    const int e = elems[grp * EG + el];
     H M[3][3], adj[3][3];
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -454,7 +455,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, int grp, bool p4_fir
   for (int t = tid; t < (P.res_only ? 0 : EG * NG); t += C::THREADS) {
     const int el = t / NG;
     if (el >= nvalid) continue;
-    const int e = P.elems[grp * EG + el];
+    const int e = elems[grp * EG + el];
     const float* f32 = &s_f32[t * 24];
     float Ff[3][3], cf[4], Cf[6][6], Sf[6], inv[3][3];
 #pragma unroll

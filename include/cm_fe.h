@@ -192,7 +192,10 @@ int fe_element_jacobians(fe_handle h, const double* x, int32_t first, int32_t co
  * member handles must outlive the batch; members with a surface-pressure
  * load get their boundary faces after each colour's volume work (a second
  * grid barrier per colour); the residual and coupling blocks are computed in
- * FP64. */
+ * FP64.  A batch holds at most 256 members (FE_ERR_NOT_SUPPORTED beyond):
+ * their parameters live in one constant-memory table per device, so batched
+ * launches and replays of all batches on a device run one after another,
+ * whatever streams they are issued on. */
 typedef struct fe_batch_s* fe_batch;
 
 int fe_batch_create(const fe_handle* handles, int32_t count, fe_batch* out);
@@ -209,7 +212,7 @@ int fe_batch_check(fe_batch b, void* stream);
 /* Launch configuration: variant (elements per group for triquadratic /
  * trilinear members: 0 = 4/8, 1 = 4/4, 2 = 2/4, 3 = 2/2, 4 = 3/2 compiled for
  * three CTAs per SM), CTAs per SM, and
- * element groups per work item (the colour-block size). */
+ * consecutive element groups per work unit. */
 int fe_batch_set_config(fe_batch b, int32_t variant, int32_t ctas_per_sm, int32_t block_groups);
 int fe_batch_get_config(fe_batch b, int32_t* variant, int32_t* ctas_per_sm, int32_t* block_groups,
                         double* tuned_ms);

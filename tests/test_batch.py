@@ -147,3 +147,46 @@ def test_batch_with_surface_pressure(torch):
     batch.jacobian_evaluate_mixed(xs, vus, vcs, rs)
     batch.check(xs[0])
     _close(torch, [(vu0, vc0, r0)], vus[:1], vcs[:1], rs[:1])
+
+
+@pytest.mark.parametrize("nxi_u,pressure", [(2, "element"), (2, "node"), (3, "element"), (3, "node")])
+def test_single_type_batches(torch, nxi_u, pressure):
+    """Batches whose members all have one element type run the kernel
+    compiled for that type alone: every launch variant agrees with the
+    single-set evaluation, with and without surface loads."""
+    from cm_gb300 import EquationsSetBatch, FiniteElasticityEquationsSet
+    ms = [M.regular_box(3, 2, 2, nxi_u=nxi_u, pressure=pressure, law=M.MR, materials=(2.0, 6.0), perturb=0.1, seed=1),
+          M.regular_box(2, 2, 3, nxi_u=nxi_u, pressure=pressure, law=M.MR, materials=(0.7, 5.0)),
+          M.regular_box(2, 3, 2, lengths=(2.0, 1.0, 0.5), nxi_u=nxi_u, pressure=pressure, law=M.GUCCIONE,
+                        materials=(0.88, 18.5, 3.58, 1.63), fibre=np.array([[0.3], [0.1], [-0.2]]))]
+    sets = [FiniteElasticityEquationsSet(m) for m in ms]
+    sp = np.zeros((3, ms[2].nu))
+    sp[2, ms[2].node_ijk()[2] == 0] = 0.8
+    sets[2].set_surface_pressure(sp)
+    xs = [torch.from_numpy(M.deformed_state(m, stretch=1.03, shear=0.02, noise=0.02, seed=i + 3)).cuda()
+          for i, m in enumerate(ms)]
+    refs = []
+    for s, x in zip(sets, xs):
+        r = torch.empty_like(x)
+        vu, vc = s.jacobian_evaluate_mixed(x, r=r)
+        s.check_status(x)
+        refs.append((vu.clone(), vc.clone(), r.clone()))
+    batch = EquationsSetBatch(sets)
+    vus, vcs, rs = batch.allocate("cuda")
+    for variant in range(5):
+        for cps in (1, 3):
+            batch.set_config(variant, cps, 2)
+            for t in vus + vcs + rs:
+                t.fill_(float("nan"))
+            batch.jacobian_evaluate_mixed(xs, vus, vcs, rs)
+            batch.check(xs[0])
+            _close(torch, refs, vus, vcs, rs)
+
+
+def test_batch_member_limit(torch):
+    from cm_gb300 import EquationsSetBatch, FEError, FiniteElasticityEquationsSet
+    es = FiniteElasticityEquationsSet(M.regular_box(1, 1, 1, nxi_u=2, pressure="element", law=M.MR,
+                                                    materials=(2.0, 6.0)))
+    EquationsSetBatch([es] * 256).close()
+    with pytest.raises(FEError):
+        EquationsSetBatch([es] * 257)
