@@ -49,8 +49,8 @@ constexpr int align16(int x) { return (x + 15) & ~15; }
 // Default elements per group: 3 for triquadratic elements with nodal pressure
 // (about 72 KB of shared memory, so three 256-thread CTAs fit on an SM, which
 // measured 17 % faster than two CTAs of 4 elements despite the register
-// spills the 80-register budget causes), 4 for element-based pressure (which
-// also keeps the FP64 gradient table), 8 for trilinear elements.
+// spills the 80-register budget causes), 4 for element-based pressure, 8 for
+// trilinear elements.
 template <int N1, int PM, int EG_ = (N1 == 3 ? (PM ? 3 : 4) : 8)>
 struct MixCfg {
   static constexpr int MINB = (N1 == 3 && PM) ? 3 : 2;  // CTAs per SM the launch bounds ask for
@@ -71,12 +71,12 @@ struct MixCfg {
   static constexpr int REC32 = 60;  // D^{mn}(k,l) for 6 blocks, padded so Gauss points 2 apart hit banks 24 apart
   static constexpr int PHS = 84;    // per-Gauss-point stride of the FP32 gradient table (conflict-free fragment loads)
   static constexpr int KAP = 84;    // contraction length: kappa = 28 k + g, g < 27 (g = 27 is padding)
-  static constexpr int O_PHI64 = 0;
-  static constexpr int O_PSI64 = align16(O_PHI64 + (PM ? 0 : NG * 4 * NPE * 8));  // FP64 gradient table: element-based pressure only
+  static constexpr int O_PSI64 = 0;
   static constexpr int O_L = align16(O_PSI64 + NG * 8 * 8);
   static constexpr int O_W = align16(O_L + 6 * 8);
   static constexpr int O_1D = align16(O_W + NG * 8);
-  static constexpr int O_Z = align16(O_1D + 6 * N1 * 8);
+  static constexpr int O_LM = align16(O_1D + 6 * N1 * 8);  // L x (1-D value | derivative) products
+  static constexpr int O_Z = align16(O_LM + 12 * N1 * 8);
   static constexpr int O_P = align16(O_Z + EG * 3 * NPE * 8);
   static constexpr int O_DZ = align16(O_P + EG * 8 * 8);
   static constexpr int O_PG = align16(O_DZ + EG * NG * 9 * 8);
@@ -200,6 +200,23 @@ __device__ __forceinline__ void load_geo(const KParams& P, int e, int g, dd dn[9
   jx = {v.x, v.y};
 }
 
+// The 3-point Gauss-Legendre abscissae on [0, 1].
+__device__ __forceinline__ double gauss_1d(int gi) {
+  return gi == 0 ? (-sqrt(0.6) + 1.0) / 2.0 : (gi == 1 ? 0.5 : (sqrt(0.6) + 1.0) / 2.0);
+}
+
+// 1-D Lagrange basis function a of degree N1 - 1 on [0, 1] and its derivative at t.
+template <int N1>
+__device__ __forceinline__ void lagrange_1d(int a, double t, double& bv, double& dv) {
+  if (N1 == 2) {
+    bv = a == 0 ? 1.0 - t : t;
+    dv = a == 0 ? -1.0 : 1.0;
+  } else {
+    bv = a == 0 ? 1.0 - 3.0 * t + 2.0 * t * t : (a == 1 ? 4.0 * t * (1.0 - t) : t * (t + t - 1.0));
+    dv = a == 0 ? 4.0 * t - 3.0 : (a == 1 ? 4.0 - 8.0 * t : 4.0 * t - 1.0);
+  }
+}
+
 // Constant tables (basis values and derivatives at the Gauss points, the
 // split BF16 gradient table of the tensor-core stage) into shared memory.
 template <int N1, int PM, int EG_, class H>
@@ -207,12 +224,12 @@ __device__ __forceinline__ void mix_tables(const KParams& P, unsigned char* sm) 
   using C = MixCfg<N1, PM, EG_>;
   constexpr int NPE = C::NPE, NPP = C::NPP, NR = C::NR, NU3 = C::NU3, NROW = C::NROW, EG = C::EG;
   constexpr int KPW = C::KPW;
-  H* s_phi = reinterpret_cast<H*>(sm + C::O_PHI64);  // [g][d][a]
   H* s_psi = reinterpret_cast<H*>(sm + C::O_PSI64);  // [g][q]
   H* s_L = reinterpret_cast<H*>(sm + C::O_L);        // [q][gi]
   H* s_w = reinterpret_cast<H*>(sm + C::O_W);        // [g]
   H* s_B1 = reinterpret_cast<H*>(sm + C::O_1D);      // [gi][a] 1-D values
   H* s_D1 = s_B1 + 3 * N1;                                // [gi][a] 1-D derivatives
+  H* s_LM = reinterpret_cast<H*>(sm + C::O_LM);      // [B|D][q][gi][a]: L(q, gi) x 1-D value | derivative
   H* s_z = reinterpret_cast<H*>(sm + C::O_Z);        // [el][c][a]
   H* s_p = reinterpret_cast<H*>(sm + C::O_P);        // [el][q]
   H* s_dz = reinterpret_cast<H*>(sm + C::O_DZ);      // [el][g][c*3+k]
@@ -226,29 +243,26 @@ __device__ __forceinline__ void mix_tables(const KParams& P, unsigned char* sm) 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nu = P.nu;
   // ---- constant tables
-  if (!PM)  // read only by the element-based pressure coupling
-    for (int i = tid; i < NG * 4 * NPE; i += C::THREADS) s_phi[i] = hval<H>(P.gbf_u[i]);
   for (int i = tid; i < NG * 8; i += C::THREADS) s_psi[i] = hval<H>(P.gbf_p[i]);
   for (int i = tid; i < NG; i += C::THREADS) s_w[i] = hval<H>(P.gw[i]);
   if (tid < 6) {
-    const double x[3] = {(-sqrt(0.6) + 1.0) / 2.0, 0.5, (sqrt(0.6) + 1.0) / 2.0};
     const int q = tid / 3, gi = tid % 3;
-    s_L[tid] = hval<H>(q == 0 ? 1.0 - x[gi] : x[gi]);
+    const double t = gauss_1d(gi);
+    s_L[tid] = hval<H>(q == 0 ? 1.0 - t : t);
   }
   if (tid < 3 * N1) {  // 1-D Lagrange values and derivatives at the Gauss points
-    const double x[3] = {(-sqrt(0.6) + 1.0) / 2.0, 0.5, (sqrt(0.6) + 1.0) / 2.0};
     const int gi = tid / N1, a = tid % N1;
-    const double t = x[gi];
     double bv, dv;
-    if (N1 == 2) {
-      bv = a == 0 ? 1.0 - t : t;
-      dv = a == 0 ? -1.0 : 1.0;
-    } else {
-      bv = a == 0 ? 1.0 - 3.0 * t + 2.0 * t * t : (a == 1 ? 4.0 * t * (1.0 - t) : t * (t + t - 1.0));
-      dv = a == 0 ? 4.0 * t - 3.0 : (a == 1 ? 4.0 - 8.0 * t : 4.0 * t - 1.0);
-    }
+    lagrange_1d<N1>(a, gauss_1d(gi), bv, dv);
     s_B1[tid] = hval<H>(bv);
     s_D1[tid] = hval<H>(dv);
+  }
+  if (tid < 12 * N1) {  // their products with the linear pressure basis (nodal-pressure coupling)
+    const int a = tid % N1, gi = (tid / N1) % 3, q = (tid / (3 * N1)) % 2, d = tid / (6 * N1);
+    const double t = gauss_1d(gi);
+    double bv, dv;
+    lagrange_1d<N1>(a, t, bv, dv);
+    s_LM[tid] = hval<H>((q == 0 ? 1.0 - t : t) * (d ? dv : bv));
   }
   for (int i = tid; i < NG * 3 * NPE; i += C::THREADS) {
     const int g = i / (3 * NPE), l = (i / NPE) % 3, b = i % NPE;
@@ -279,12 +293,12 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
   using C = MixCfg<N1, PM, EG_>;
   constexpr int NPE = C::NPE, NPP = C::NPP, NR = C::NR, NU3 = C::NU3, NROW = C::NROW, EG = C::EG;
   constexpr int KPW = C::KPW;
-  H* s_phi = reinterpret_cast<H*>(sm + C::O_PHI64);  // [g][d][a]
   H* s_psi = reinterpret_cast<H*>(sm + C::O_PSI64);  // [g][q]
   H* s_L = reinterpret_cast<H*>(sm + C::O_L);        // [q][gi]
   H* s_w = reinterpret_cast<H*>(sm + C::O_W);        // [g]
   H* s_B1 = reinterpret_cast<H*>(sm + C::O_1D);      // [gi][a] 1-D values
   H* s_D1 = s_B1 + 3 * N1;                                // [gi][a] 1-D derivatives
+  H* s_LM = reinterpret_cast<H*>(sm + C::O_LM);      // [B|D][q][gi][a]: L(q, gi) x 1-D value | derivative
   H* s_z = reinterpret_cast<H*>(sm + C::O_Z);        // [el][c][a]
   H* s_p = reinterpret_cast<H*>(sm + C::O_P);        // [el][q]
   H* s_dz = reinterpret_cast<H*>(sm + C::O_DZ);      // [el][g][c*3+k]
@@ -501,12 +515,15 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
     if ((ph == 0) != p4_first) {
       // ---- P3: residual rows and pressure-coupling columns (high precision H)
       __syncthreads();
-      if (P.r != nullptr) {
-        // Displacement rows by sum factorisation over the tensor-product basis:
-        // r(m, a) = sum_k sum_g M_k(g; a) P_g(k, m) with M_k the product of the
-        // 1-D derivative table along xi_k and the 1-D value table along the
-        // other two directions; one xi direction contracted per stage.
-        constexpr int N2 = N1 * N1;
+      // Sum factorisation over the tensor-product basis:
+      //   RK[el][mk][a] = sum_g M_k(g; a) V_g(k, m),  V_g(k, m) = rec_g[roff + 3 k + m],
+      // with M_k the product of the 1-D derivative table along xi_k and the
+      // 1-D value table along the other two directions; one xi direction
+      // contracted per stage.  roff = 0: V = P, the residual rows are
+      // sum_k RK; roff = 9: V = A = J_z w dxi/dz, the element-based pressure
+      // coupling column of (n, b) is sum_k RK[el][3 n + k][b].
+      constexpr int N2 = N1 * N1;
+      auto sumfact = [&](int roff) {
         H* U1 = s_dz;                         // [el][mk][a1][g2 + 3 g3]
         H* U2 = reinterpret_cast<H*>(s_f32);  // [el][mk][a1 + N1 a2][g3]
         H* RK = s_dz;                         // [el][mk][a]
@@ -514,7 +531,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
           const int j = i % 9, a1 = (i / 9) % N1, mk = (i / (9 * N1)) % 9, el = i / (81 * N1);
           const int m = mk / 3, k = mk % 3;
           const H* M = k == 0 ? s_D1 : s_B1;
-          const H* rec = &s_r64[(el * NG + 3 * j) * C::REC64 + k * 3 + m];
+          const H* rec = &s_r64[(el * NG + 3 * j) * C::REC64 + roff + k * 3 + m];
           H acc = hval<H>(0.0);
 #pragma unroll
           for (int g1 = 0; g1 < 3; ++g1) acc = hfma(M[g1 * N1 + a1], rec[g1 * C::REC64], acc);
@@ -543,11 +560,10 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
           RK[i] = acc;
         }
         __syncthreads();
-      }
-      const int n_res = P.r != nullptr ? EG * NROW : 0;
-      const int n_cp = (P.res_only || PM) ? 0 : EG * NU3;  // nodal pressure: sum-factorised loop below
-      for (int it = tid; it < n_res + n_cp; it += C::THREADS) {
-        if (it < n_res) {
+      };
+      if (P.r != nullptr) {
+        sumfact(0);
+        for (int it = tid; it < EG * NROW; it += C::THREADS) {
           const int el = it / NROW, row = it % NROW;
           if (el >= nvalid) continue;
           const H* rec = &s_r64[el * NG * C::REC64];
@@ -575,140 +591,92 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
             P.r[R] = accd;
           else
             atomicAdd(&P.r[R], accd);
-        } else {
-          const int j = it - n_res;
-          const int el = j / NU3, col = j % NU3;
-          if (el >= nvalid) continue;
-          const int n = col / NPE, b = col % NPE;
-          const H* rec = &s_r64[el * NG * C::REC64];
-          const int* nd = &s_node[el * (NR + 1)];
-          const uint16_t* tab = P.tables + (size_t)nd[NR] * NR * NR;
-          // V(g) = J_z w dN_b/dz_n at Gauss point g, folded into the xi1 stage
-          // of the sum-factorised pressure-basis contraction as it is produced.
-          H Kq[NPP];
-          H s1[2][9];
-          H vsum = hval<H>(0.0);
-#pragma unroll
-          for (int jj = 0; jj < 9; ++jj) {
-            H v3[3];
-#pragma unroll
-            for (int g1 = 0; g1 < 3; ++g1) {
-              const int g = g1 + 3 * jj;
-              const H* ph = &s_phi[g * 4 * NPE + b];
-              const H* rg = &rec[g * C::REC64 + 9];
-              v3[g1] = hfma(rg[n], ph[NPE], hfma(rg[3 + n], ph[2 * NPE], rg[6 + n] * ph[3 * NPE]));
-            }
-            if (PM) {
-#pragma unroll
-              for (int q1 = 0; q1 < 2; ++q1)
-                s1[q1][jj] = hfma(s_L[q1 * 3], v3[0], hfma(s_L[q1 * 3 + 1], v3[1], s_L[q1 * 3 + 2] * v3[2]));
-            } else {
-              vsum = vsum + v3[0] + v3[1] + v3[2];
-            }
-          }
-          if (PM) {
-            H s2[2][2][3];
-#pragma unroll
-            for (int q1 = 0; q1 < 2; ++q1)
-#pragma unroll
-              for (int q2 = 0; q2 < 2; ++q2)
-#pragma unroll
-                for (int g3 = 0; g3 < 3; ++g3)
-                  s2[q1][q2][g3] = hfma(s_L[q2 * 3], s1[q1][3 * g3],
-                                        hfma(s_L[q2 * 3 + 1], s1[q1][3 * g3 + 1], s_L[q2 * 3 + 2] * s1[q1][3 * g3 + 2]));
-#pragma unroll
-            for (int q = 0; q < NPP; ++q) {
-              const int q1 = q & 1, q2 = (q >> 1) & 1, q3 = q >> 2;
-              Kq[q] = hfma(s_L[q3 * 3], s2[q1][q2][0], hfma(s_L[q3 * 3 + 1], s2[q1][q2][1], s_L[q3 * 3 + 2] * s2[q1][q2][2]));
-            }
-          } else {
-            Kq[0] = vsum;
-          }
-          const int nb = nd[b];
-#pragma unroll
-          for (int q = 0; q < NPP; ++q) {
-            const int lq = NPE + q, pq = nd[lq];
-            const uint16_t tqb = tab[lq * NR + b], tbq = tab[b * NR + lq];
-            const double kv = hd(Kq[q]);
-            const size_t p1 = (size_t)P.cp_row_ptr[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (tqb & 0x7fff);
-            if ((tqb & 0x8000))
-              P.vals[p1] = kv;
-            else
-              atomicAdd(&P.vals[p1], kv);
-            const size_t p2 = (size_t)P.cp_row_ptr[(size_t)n * nu + nb] + (tbq & 0x7fff);
-            if ((tbq & 0x8000))
-              P.vals[p2] = kv;
-            else
-              atomicAdd(&P.vals[p2], kv);
-          }
         }
       }
-      // Pressure-coupling block for nodal (trilinear) pressure by sum
-      // factorisation over both tensor-product bases:
-      //   K(q, n, b) = sum_k sum_g psi_q(g) A_g(k, n) dN_b/dxi_k(g),  A_g = J_z w dxi/dz,
-      // with psi_q = L(q1) L(q2) L(q3) and dN_b/dxi_k = M1k(b1) M2k(b2) M3k(b3)
-      // (M = 1-D derivative along xi_k, 1-D value otherwise), contracting
-      // g1, then g2, then g3.  One thread per (element, n, q1, b1, q2).
-      if (PM && !P.res_only) {
-        for (int t = tid; t < EG * 12 * N1; t += C::THREADS) {
-          const int q2 = t % 2, b1 = (t / 2) % N1, q1 = (t / (2 * N1)) % 2, n = (t / (4 * N1)) % 3,
-                    el = t / (12 * N1);
+      if (!PM && !P.res_only) {
+        __syncthreads();  // the residual rows have read RK
+        sumfact(9);
+        for (int it = tid; it < EG * NU3; it += C::THREADS) {
+          const int el = it / NU3, col = it % NU3;
           if (el >= nvalid) continue;
-          const H* rec = &s_r64[el * NG * C::REC64 + 9 + n];
-          H out[N1][2][N1];
-#pragma unroll
-          for (int b2 = 0; b2 < N1; ++b2)
-#pragma unroll
-            for (int q3 = 0; q3 < 2; ++q3)
-#pragma unroll
-              for (int b3 = 0; b3 < N1; ++b3) out[b2][q3][b3] = hval<H>(0.0);
-#pragma unroll 1
-          for (int k = 0; k < 3; ++k) {
-            const H* M1 = k == 0 ? s_D1 : s_B1;
-            const H* M2 = k == 1 ? s_D1 : s_B1;
-            const H* M3 = k == 2 ? s_D1 : s_B1;
-            H c1[3];
-#pragma unroll
-            for (int g1 = 0; g1 < 3; ++g1) c1[g1] = s_L[q1 * 3 + g1] * M1[g1 * N1 + b1];
-            H u1[9];  // g2 + 3 g3
-#pragma unroll
-            for (int j = 0; j < 9; ++j) {
-              const H* tg = &rec[(3 * j) * C::REC64 + 3 * k];
-              u1[j] = hfma(c1[0], tg[0], hfma(c1[1], tg[C::REC64], c1[2] * tg[2 * C::REC64]));
-            }
-#pragma unroll
-            for (int b2 = 0; b2 < N1; ++b2) {
-              H u2[3];  // g3
-#pragma unroll
-              for (int g3 = 0; g3 < 3; ++g3) {
-                H acc = hval<H>(0.0);
-#pragma unroll
-                for (int g2 = 0; g2 < 3; ++g2) acc = hfma(s_L[q2 * 3 + g2] * M2[g2 * N1 + b2], u1[g2 + 3 * g3], acc);
-                u2[g3] = acc;
-              }
-#pragma unroll
-              for (int q3 = 0; q3 < 2; ++q3)
-#pragma unroll
-                for (int b3 = 0; b3 < N1; ++b3) {
-                  H acc = out[b2][q3][b3];
-#pragma unroll
-                  for (int g3 = 0; g3 < 3; ++g3) acc = hfma(s_L[q3 * 3 + g3] * M3[g3 * N1 + b3], u2[g3], acc);
-                  out[b2][q3][b3] = acc;
-                }
-            }
-          }
+          const int n = col / NPE, b = col % NPE;
           const int* nd = &s_node[el * (NR + 1)];
           const uint16_t* tab = P.tables + (size_t)nd[NR] * NR * NR;
+          const H* rk = &s_dz[(el * 9 + n * 3) * NPE + b];
+          const double kv = hd(rk[0] + rk[NPE] + rk[2 * NPE]);
+          const int nb = nd[b], pq = nd[NPE];
+          const uint16_t tqb = tab[NPE * NR + b], tbq = tab[b * NR + NPE];
+          const size_t p1 = (size_t)P.cp_row_ptr[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (tqb & 0x7fff);
+          if (tqb & 0x8000)
+            P.vals[p1] = kv;
+          else
+            atomicAdd(&P.vals[p1], kv);
+          const size_t p2 = (size_t)P.cp_row_ptr[(size_t)n * nu + nb] + (tbq & 0x7fff);
+          if (tbq & 0x8000)
+            P.vals[p2] = kv;
+          else
+            atomicAdd(&P.vals[p2], kv);
+        }
+      }
+      // Pressure-coupling block for nodal (trilinear) pressure,
+      //   K(q, n, b) = sum_k sum_g psi_q(g) A_g(k, n) dN_b/dxi_k(g),  A_g = J_z w dxi/dz,
+      // psi_q = L(q1) L(q2) L(q3), dN_b/dxi_k = M1k(b1) M2k(b2) M3k(b3) (M = 1-D
+      // derivative along xi_k, 1-D value otherwise), by sum factorisation with
+      // the products LB = L x value, LD = L x derivative of the 1-D tables.
+      // For each n: stage 1 contracts g1 for every k into
+      // T1[el][k][q1][b1][g2 + 3 g3]; then one thread per (el, q1, b1, q2, b2)
+      // contracts g2 -- the k = 0 and k = 1 terms, which share the value table
+      // along xi3, summed into w, the k = 2 term into u -- and g3.
+      if (PM && !P.res_only) {
+        constexpr int NT1 = 3 * 2 * N1 * 9;  // T1 entries per element
+        H* T1 = reinterpret_cast<H*>(s_f32);
+        const H* LB = s_LM;
+        const H* LD = s_LM + 6 * N1;
+        for (int n = 0; n < 3; ++n) {
+          __syncthreads();  // the previous readers of this region are done
+          for (int i = tid; i < EG * NT1; i += C::THREADS) {
+            const int j = i % 9, b1 = (i / 9) % N1, q1 = (i / (9 * N1)) % 2, k = (i / (18 * N1)) % 3,
+                      el = i / NT1;
+            const H* lm = (k == 0 ? LD : LB) + q1 * 3 * N1 + b1;
+            const H* a = &s_r64[(el * NG + 3 * j) * C::REC64 + 9 + 3 * k + n];
+            T1[i] = hfma(lm[0], a[0], hfma(lm[N1], a[C::REC64], lm[2 * N1] * a[2 * C::REC64]));
+          }
+          __syncthreads();
+          for (int t = tid; t < EG * 4 * N2; t += C::THREADS) {
+            const int b2 = t % N1, q2 = (t / N1) % 2, b1 = (t / (2 * N1)) % N1, q1 = (t / (2 * N2)) % 2,
+                      el = t / (4 * N2);
+            if (el >= nvalid) continue;
+            const H* t0 = &T1[el * NT1 + (q1 * N1 + b1) * 9];  // k stride 18 N1
+            const H* lb2 = LB + q2 * 3 * N1 + b2;
+            const H* ld2 = LD + q2 * 3 * N1 + b2;
+            H w[3], u[3];
 #pragma unroll
-          for (int b2 = 0; b2 < N1; ++b2)
+            for (int g3 = 0; g3 < 3; ++g3) {
+              H wa = hval<H>(0.0), ua = hval<H>(0.0);
+#pragma unroll
+              for (int g2 = 0; g2 < 3; ++g2) {
+                const int jj = g2 + 3 * g3;
+                wa = hfma(lb2[g2 * N1], t0[jj], wa);
+                wa = hfma(ld2[g2 * N1], t0[18 * N1 + jj], wa);
+                ua = hfma(lb2[g2 * N1], t0[36 * N1 + jj], ua);
+              }
+              w[g3] = wa;
+              u[g3] = ua;
+            }
+            const int* nd = &s_node[el * (NR + 1)];
+            const uint16_t* tab = P.tables + (size_t)nd[NR] * NR * NR;
 #pragma unroll
             for (int q3 = 0; q3 < 2; ++q3)
 #pragma unroll
               for (int b3 = 0; b3 < N1; ++b3) {
-                const int q = q1 + 2 * q2 + 4 * q3, b = b1 + N1 * b2 + N1 * N1 * b3;
+                H acc = hval<H>(0.0);
+#pragma unroll
+                for (int g3 = 0; g3 < 3; ++g3)
+                  acc = hfma(LD[(q3 * 3 + g3) * N1 + b3], u[g3], hfma(LB[(q3 * 3 + g3) * N1 + b3], w[g3], acc));
+                const int q = q1 + 2 * q2 + 4 * q3, b = b1 + N1 * b2 + N2 * b3;
                 const int lq = NPE + q, pq = nd[lq], nb = nd[b];
                 const uint16_t tqb = tab[lq * NR + b], tbq = tab[b * NR + lq];
-                const double kv = hd(out[b2][q3][b3]);
+                const double kv = hd(acc);
                 const size_t p1 = (size_t)P.cp_row_ptr[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (tqb & 0x7fff);
                 if (tqb & 0x8000)
                   P.vals[p1] = kv;
@@ -720,6 +688,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
                 else
                   atomicAdd(&P.vals[p2], kv);
               }
+          }
         }
       }
       // structurally zero pressure-pressure entries, stored by their first contributor
