@@ -393,119 +393,135 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
     s_pg[i] = pg;
   }
   __syncthreads();
-  // ---- P2: per Gauss point kinematics and stress in H, hand-off to FP32
-  for (int t = tid; t < EG * NG; t += C::THREADS) {
-    const int el = t / NG, g = t % NG;
-    if (el >= nvalid) continue;
-    const int e = elems[grp * EG + el];
-    H M[3][3], adj[3][3];
+  // ---- P2 (H: kinematics, stress and the residual / coupling records per
+  // Gauss point) and P2b (FP32: the spatial tangent pulled back to xi space)
+  // run at the same time on the two halves of the CTA, so that the FP64 and
+  // the FP32 pipes overlap; P2b forms the FP32 kinematics it needs itself from
+  // the same gradients.
+  constexpr int HALF = C::THREADS / 2;
+  if (tid < HALF) {
+    for (int t = tid; t < EG * NG; t += HALF) {
+      const int el = t / NG, g = t % NG;
+      if (el >= nvalid) continue;
+      const int e = elems[grp * EG + el];
+      H M[3][3], adj[3][3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c)
+      for (int c = 0; c < 3; ++c)
 #pragma unroll
-      for (int k = 0; k < 3; ++k) M[c][k] = s_dz[t * 9 + c * 3 + k];
-    adj[0][0] = M[1][1] * M[2][2] - M[1][2] * M[2][1];
-    adj[0][1] = M[0][2] * M[2][1] - M[0][1] * M[2][2];
-    adj[0][2] = M[0][1] * M[1][2] - M[0][2] * M[1][1];
-    adj[1][0] = M[1][2] * M[2][0] - M[1][0] * M[2][2];
-    adj[1][1] = M[0][0] * M[2][2] - M[0][2] * M[2][0];
-    adj[1][2] = M[0][2] * M[1][0] - M[0][0] * M[1][2];
-    adj[2][0] = M[1][0] * M[2][1] - M[1][1] * M[2][0];
-    adj[2][1] = M[0][1] * M[2][0] - M[0][0] * M[2][1];
-    adj[2][2] = M[0][0] * M[1][1] - M[0][1] * M[1][0];
-    const H det = M[0][0] * adj[0][0] + M[0][1] * adj[1][0] + M[0][2] * adj[2][0];
-    H dn[9], jx;
-    load_geo(P, e, g, dn, jx);
-    H F[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) F[i][j] = M[i][0] * dn[j] + M[i][1] * dn[3 + j] + M[i][2] * dn[6 + j];
-    const H jz = habs(det);
-    const H jznu = jz / jx;
-    const H w = s_w[g];
-    const bool dpos = hpos(det);
-    const H sw = dpos ? w : -w;  // J_z w dxi/dz = sign(det) w adj
-    const double* cm = P.mat + (P.matpe ? (size_t)e * P.nmat : 0);
-    const H cc[4] = {hval<H>(cm[0]), hval<H>(cm[1]), hval<H>(P.nmat > 2 ? cm[2] : 0.0),
-                     hval<H>(P.nmat > 3 ? cm[3] : 0.0)};
-    const H pgv = s_pg[t];
-    H* rec = &s_r64[t * C::REC64];
-    bool ok = dpos;
-    if (P.r != nullptr) {
-      H sig[3][3];
-      mix_stress<H>(P.law, cc, F, jznu, pgv, sig);
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int m = 0; m < 3; ++m) {
-          const H v = sw * (adj[k][0] * sig[0][m] + adj[k][1] * sig[1][m] + adj[k][2] * sig[2][m]);
-          rec[k * 3 + m] = v;
-          ok = ok && hfinite(v);
-        }
-      rec[18] = jx * w * (jznu - hval<H>(1.0));
-    }
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-#pragma unroll
-      for (int n = 0; n < 3; ++n) rec[9 + k * 3 + n] = sw * adj[k][n];
-    if (!ok) atomicOr(P.status, 1u);
-    if (P.res_only) continue;
-    // hand-off to the FP32 tangent stage
-    float* f32 = &s_f32[t * 24];
-    const float rdet = 1.0f / hf(det);
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        f32[i * 3 + j] = hf(F[i][j]);
-        f32[9 + i * 3 + j] = hf(adj[i][j]) * rdet;
-      }
-    f32[18] = hf(jz * w);
-    f32[19] = hf(jznu);
-    f32[20] = hf(pgv);
-  }
-  __syncthreads();
-  // ---- P2b: FP32 spatial tangent pulled back to xi space, per Gauss point
-  for (int t = tid; t < (P.res_only ? 0 : EG * NG); t += C::THREADS) {
-    const int el = t / NG;
-    if (el >= nvalid) continue;
-    const int e = elems[grp * EG + el];
-    const float* f32 = &s_f32[t * 24];
-    float Ff[3][3], cf[4], Cf[6][6], Sf[6], inv[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        Ff[i][j] = f32[i * 3 + j];
-        inv[i][j] = f32[9 + i * 3 + j];
-      }
-    const double* cm = P.mat + (P.matpe ? (size_t)e * P.nmat : 0);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) cf[i] = i < P.nmat ? (float)cm[i] : 0.0f;
-    d_gauss_elasticity<float>(P.law, cf, Ff, f32[19], f32[20], Cf, Sf);
-    const float jgwf = f32[18];
-    float* r32 = &s_r32[t * C::REC32];
-#pragma unroll
-    for (int blk = 0; blk < 6; ++blk) {
-      int m, n;
-      blk_mn(blk, m, n);
-      float sub[3][3], tmp[3][3];
+        for (int k = 0; k < 3; ++k) M[c][k] = s_dz[t * 9 + c * 3 + k];
+      adj[0][0] = M[1][1] * M[2][2] - M[1][2] * M[2][1];
+      adj[0][1] = M[0][2] * M[2][1] - M[0][1] * M[2][2];
+      adj[0][2] = M[0][1] * M[1][2] - M[0][2] * M[1][1];
+      adj[1][0] = M[1][2] * M[2][0] - M[1][0] * M[2][2];
+      adj[1][1] = M[0][0] * M[2][2] - M[0][2] * M[2][0];
+      adj[1][2] = M[0][2] * M[1][0] - M[0][0] * M[1][2];
+      adj[2][0] = M[1][0] * M[2][1] - M[1][1] * M[2][0];
+      adj[2][1] = M[0][1] * M[2][0] - M[0][0] * M[2][1];
+      adj[2][2] = M[0][0] * M[1][1] - M[0][1] * M[1][0];
+      const H det = M[0][0] * adj[0][0] + M[0][1] * adj[1][0] + M[0][2] * adj[2][0];
+      H dn[9], jx;
+      load_geo(P, e, g, dn, jx);
+      H F[3][3];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j)
-          sub[i][j] = jgwf * (Cf[t2v(i, m)][t2v(j, n)] + (m == n ? Sf[t2v(i, j)] : 0.0f));
+        for (int j = 0; j < 3; ++j) F[i][j] = M[i][0] * dn[j] + M[i][1] * dn[3 + j] + M[i][2] * dn[6 + j];
+      const H jz = habs(det);
+      const H jznu = jz / jx;
+      const H w = s_w[g];
+      const bool dpos = hpos(det);
+      const H sw = dpos ? w : -w;  // J_z w dxi/dz = sign(det) w adj
+      const double* cm = P.mat + (P.matpe ? (size_t)e * P.nmat : 0);
+      const H cc[4] = {hval<H>(cm[0]), hval<H>(cm[1]), hval<H>(P.nmat > 2 ? cm[2] : 0.0),
+                       hval<H>(P.nmat > 3 ? cm[3] : 0.0)};
+      const H pgv = s_pg[t];
+      H* rec = &s_r64[t * C::REC64];
+      bool ok = dpos;
+      if (P.r != nullptr) {
+        H sig[3][3];
+        mix_stress<H>(P.law, cc, F, jznu, pgv, sig);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            const H v = sw * (adj[k][0] * sig[0][m] + adj[k][1] * sig[1][m] + adj[k][2] * sig[2][m]);
+            rec[k * 3 + m] = v;
+            ok = ok && hfinite(v);
+          }
+        rec[18] = jx * w * (jznu - hval<H>(1.0));
+      }
 #pragma unroll
       for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) tmp[k][j] = inv[k][0] * sub[0][j] + inv[k][1] * sub[1][j] + inv[k][2] * sub[2][j];
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int l = 0; l < 3; ++l)
-          r32[blk * 9 + k * 3 + l] = tmp[k][0] * inv[l][0] + tmp[k][1] * inv[l][1] + tmp[k][2] * inv[l][2];
+        for (int n = 0; n < 3; ++n) rec[9 + k * 3 + n] = sw * adj[k][n];
+      if (!ok) atomicOr(P.status, 1u);
     }
-    if (!(isfinite(Cf[0][0]) && isfinite(Cf[3][3]))) atomicOr(P.status, 1u);
+  } else {
+    for (int t = tid - HALF; t < (P.res_only ? 0 : EG * NG); t += HALF) {
+      const int el = t / NG, g = t % NG;
+      if (el >= nvalid) continue;
+      const int e = elems[grp * EG + el];
+      float Mf[3][3], Ff[3][3], cf[4], Cf[6][6], Sf[6], inv[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) Mf[c][k] = hf(s_dz[t * 9 + c * 3 + k]);
+      H dnh[9], jxh;
+      load_geo(P, e, g, dnh, jxh);
+      float dn[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) dn[i] = hf(dnh[i]);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Ff[i][j] = Mf[i][0] * dn[j] + Mf[i][1] * dn[3 + j] + Mf[i][2] * dn[6 + j];
+      float adj[3][3];
+      adj[0][0] = Mf[1][1] * Mf[2][2] - Mf[1][2] * Mf[2][1];
+      adj[0][1] = Mf[0][2] * Mf[2][1] - Mf[0][1] * Mf[2][2];
+      adj[0][2] = Mf[0][1] * Mf[1][2] - Mf[0][2] * Mf[1][1];
+      adj[1][0] = Mf[1][2] * Mf[2][0] - Mf[1][0] * Mf[2][2];
+      adj[1][1] = Mf[0][0] * Mf[2][2] - Mf[0][2] * Mf[2][0];
+      adj[1][2] = Mf[0][2] * Mf[1][0] - Mf[0][0] * Mf[1][2];
+      adj[2][0] = Mf[1][0] * Mf[2][1] - Mf[1][1] * Mf[2][0];
+      adj[2][1] = Mf[0][1] * Mf[2][0] - Mf[0][0] * Mf[2][1];
+      adj[2][2] = Mf[0][0] * Mf[1][1] - Mf[0][1] * Mf[1][0];
+      const float det = Mf[0][0] * adj[0][0] + Mf[0][1] * adj[1][0] + Mf[0][2] * adj[2][0];
+      const float rdet = 1.0f / det;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) inv[i][j] = adj[i][j] * rdet;
+      const float jz = fabsf(det);
+      const float jznuf = jz / hf(jxh);
+      const float jgwf = jz * hf(s_w[g]);
+      const float pgf = hf(s_pg[t]);
+      const double* cm = P.mat + (P.matpe ? (size_t)e * P.nmat : 0);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) cf[i] = i < P.nmat ? (float)cm[i] : 0.0f;
+      d_gauss_elasticity<float>(P.law, cf, Ff, jznuf, pgf, Cf, Sf);
+      float* r32 = &s_r32[t * C::REC32];
+#pragma unroll
+      for (int blk = 0; blk < 6; ++blk) {
+        int m, n;
+        blk_mn(blk, m, n);
+        float sub[3][3], tmp[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            sub[i][j] = jgwf * (Cf[t2v(i, m)][t2v(j, n)] + (m == n ? Sf[t2v(i, j)] : 0.0f));
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) tmp[k][j] = inv[k][0] * sub[0][j] + inv[k][1] * sub[1][j] + inv[k][2] * sub[2][j];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int l = 0; l < 3; ++l)
+            r32[blk * 9 + k * 3 + l] = tmp[k][0] * inv[l][0] + tmp[k][1] * inv[l][1] + tmp[k][2] * inv[l][2];
+      }
+      if (!(isfinite(Cf[0][0]) && isfinite(Cf[3][3]))) atomicOr(P.status, 1u);
+    }
   }
   __syncthreads();
   // P3 (FP64 pipe) and P4 (tensor cores, scatter) are independent; the
