@@ -238,7 +238,7 @@ __device__ __forceinline__ void mix_tables(const KParams& P, unsigned char* sm) 
   float* s_phi32 = reinterpret_cast<float*>(sm + C::O_PHI32);  // [g][l][b]
   float* s_r32 = reinterpret_cast<float*>(sm + C::O_R32);      // [el][g][REC32]
   uint32_t* s_A = reinterpret_cast<uint32_t*>(sm + C::O_A);    // [hi/lo][a][KPW]
-  float* s_f32 = reinterpret_cast<float*>(sm + C::O_F32);      // [el][g][24] FP32 hand-off
+  float* s_f32 = reinterpret_cast<float*>(sm + C::O_F32);      // scratch of P3 and P4 (EG x 2592 B)
   int* s_node = reinterpret_cast<int*>(sm + C::O_NODE);        // [el][NR+1]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nu = P.nu;
@@ -307,7 +307,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
   float* s_phi32 = reinterpret_cast<float*>(sm + C::O_PHI32);  // [g][l][b]
   float* s_r32 = reinterpret_cast<float*>(sm + C::O_R32);      // [el][g][REC32]
   uint32_t* s_A = reinterpret_cast<uint32_t*>(sm + C::O_A);    // [hi/lo][a][KPW]
-  float* s_f32 = reinterpret_cast<float*>(sm + C::O_F32);      // [el][g][24] FP32 hand-off
+  float* s_f32 = reinterpret_cast<float*>(sm + C::O_F32);      // scratch of P3 and P4 (EG x 2592 B)
   int* s_node = reinterpret_cast<int*>(sm + C::O_NODE);        // [el][NR+1]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nu = P.nu;
@@ -639,72 +639,75 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
       // psi_q = L(q1) L(q2) L(q3), dN_b/dxi_k = M1k(b1) M2k(b2) M3k(b3) (M = 1-D
       // derivative along xi_k, 1-D value otherwise), by sum factorisation with
       // the products LB = L x value, LD = L x derivative of the 1-D tables.
-      // For each n: stage 1 contracts g1 for every k into
-      // T1[el][k][q1][b1][g2 + 3 g3]; then one thread per (el, q1, b1, q2, b2)
+      // Stage 1 contracts g1 for every (n, k) into T1_n[el][k][q1][b1][g2 + 3 g3]
+      // (n = 0, 1 in the s_f32 scratch region, n = 2 in the gradient region,
+      // both free by now); then one thread per (n, el, q1, b1, q2, b2)
       // contracts g2 -- the k = 0 and k = 1 terms, which share the value table
       // along xi3, summed into w, the k = 2 term into u -- and g3.
       if (PM && !P.res_only) {
-        constexpr int NT1 = 3 * 2 * N1 * 9;  // T1 entries per element
-        H* T1 = reinterpret_cast<H*>(s_f32);
+        constexpr int NT1 = 3 * 2 * N1 * 9;  // T1 entries per element and n
+        H* T1f = reinterpret_cast<H*>(s_f32);
         const H* LB = s_LM;
         const H* LD = s_LM + 6 * N1;
-        for (int n = 0; n < 3; ++n) {
-          __syncthreads();  // the previous readers of this region are done
-          for (int i = tid; i < EG * NT1; i += C::THREADS) {
-            const int j = i % 9, b1 = (i / 9) % N1, q1 = (i / (9 * N1)) % 2, k = (i / (18 * N1)) % 3,
-                      el = i / NT1;
-            const H* lm = (k == 0 ? LD : LB) + q1 * 3 * N1 + b1;
-            const H* a = &s_r64[(el * NG + 3 * j) * C::REC64 + 9 + 3 * k + n];
-            T1[i] = hfma(lm[0], a[0], hfma(lm[N1], a[C::REC64], lm[2 * N1] * a[2 * C::REC64]));
-          }
-          __syncthreads();
-          for (int t = tid; t < EG * 4 * N2; t += C::THREADS) {
-            const int b2 = t % N1, q2 = (t / N1) % 2, b1 = (t / (2 * N1)) % N1, q1 = (t / (2 * N2)) % 2,
-                      el = t / (4 * N2);
-            if (el >= nvalid) continue;
-            const H* t0 = &T1[el * NT1 + (q1 * N1 + b1) * 9];  // k stride 18 N1
-            const H* lb2 = LB + q2 * 3 * N1 + b2;
-            const H* ld2 = LD + q2 * 3 * N1 + b2;
-            H w[3], u[3];
+        __syncthreads();  // the residual rows have read the gradient region
+        for (int i = tid; i < 3 * EG * NT1; i += C::THREADS) {
+          const int n = i / (EG * NT1), r = i % (EG * NT1);
+          const int j = r % 9, b1 = (r / 9) % N1, q1 = (r / (9 * N1)) % 2, k = (r / (18 * N1)) % 3,
+                    el = r / NT1;
+          const H* lm = (k == 0 ? LD : LB) + q1 * 3 * N1 + b1;
+          const H* a = &s_r64[(el * NG + 3 * j) * C::REC64 + 9 + 3 * k + n];
+          H* T1 = n < 2 ? T1f + n * EG * NT1 : s_dz;
+          T1[r] = hfma(lm[0], a[0], hfma(lm[N1], a[C::REC64], lm[2 * N1] * a[2 * C::REC64]));
+        }
+        __syncthreads();
+        for (int tt = tid; tt < 3 * EG * 4 * N2; tt += C::THREADS) {
+          const int n = tt / (EG * 4 * N2), t = tt % (EG * 4 * N2);
+          const int b2 = t % N1, q2 = (t / N1) % 2, b1 = (t / (2 * N1)) % N1, q1 = (t / (2 * N2)) % 2,
+                    el = t / (4 * N2);
+          if (el >= nvalid) continue;
+          const H* T1 = n < 2 ? T1f + n * EG * NT1 : s_dz;
+          const H* t0 = &T1[el * NT1 + (q1 * N1 + b1) * 9];  // k stride 18 N1
+          const H* lb2 = LB + q2 * 3 * N1 + b2;
+          const H* ld2 = LD + q2 * 3 * N1 + b2;
+          H w[3], u[3];
 #pragma unroll
-            for (int g3 = 0; g3 < 3; ++g3) {
-              H wa = hval<H>(0.0), ua = hval<H>(0.0);
+          for (int g3 = 0; g3 < 3; ++g3) {
+            H wa = hval<H>(0.0), ua = hval<H>(0.0);
 #pragma unroll
-              for (int g2 = 0; g2 < 3; ++g2) {
-                const int jj = g2 + 3 * g3;
-                wa = hfma(lb2[g2 * N1], t0[jj], wa);
-                wa = hfma(ld2[g2 * N1], t0[18 * N1 + jj], wa);
-                ua = hfma(lb2[g2 * N1], t0[36 * N1 + jj], ua);
-              }
-              w[g3] = wa;
-              u[g3] = ua;
+            for (int g2 = 0; g2 < 3; ++g2) {
+              const int jj = g2 + 3 * g3;
+              wa = hfma(lb2[g2 * N1], t0[jj], wa);
+              wa = hfma(ld2[g2 * N1], t0[18 * N1 + jj], wa);
+              ua = hfma(lb2[g2 * N1], t0[36 * N1 + jj], ua);
             }
-            const int* nd = &s_node[el * (NR + 1)];
-            const uint16_t* tab = P.tables + (size_t)nd[NR] * NR * NR;
-#pragma unroll
-            for (int q3 = 0; q3 < 2; ++q3)
-#pragma unroll
-              for (int b3 = 0; b3 < N1; ++b3) {
-                H acc = hval<H>(0.0);
-#pragma unroll
-                for (int g3 = 0; g3 < 3; ++g3)
-                  acc = hfma(LD[(q3 * 3 + g3) * N1 + b3], u[g3], hfma(LB[(q3 * 3 + g3) * N1 + b3], w[g3], acc));
-                const int q = q1 + 2 * q2 + 4 * q3, b = b1 + N1 * b2 + N2 * b3;
-                const int lq = NPE + q, pq = nd[lq], nb = nd[b];
-                const uint16_t tqb = tab[lq * NR + b], tbq = tab[b * NR + lq];
-                const double kv = hd(acc);
-                const size_t p1 = (size_t)P.cp_row_ptr[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (tqb & 0x7fff);
-                if (tqb & 0x8000)
-                  P.vals[p1] = kv;
-                else
-                  atomicAdd(&P.vals[p1], kv);
-                const size_t p2 = (size_t)P.cp_row_ptr[(size_t)n * nu + nb] + (tbq & 0x7fff);
-                if (tbq & 0x8000)
-                  P.vals[p2] = kv;
-                else
-                  atomicAdd(&P.vals[p2], kv);
-              }
+            w[g3] = wa;
+            u[g3] = ua;
           }
+          const int* nd = &s_node[el * (NR + 1)];
+          const uint16_t* tab = P.tables + (size_t)nd[NR] * NR * NR;
+#pragma unroll
+          for (int q3 = 0; q3 < 2; ++q3)
+#pragma unroll
+            for (int b3 = 0; b3 < N1; ++b3) {
+              H acc = hval<H>(0.0);
+#pragma unroll
+              for (int g3 = 0; g3 < 3; ++g3)
+                acc = hfma(LD[(q3 * 3 + g3) * N1 + b3], u[g3], hfma(LB[(q3 * 3 + g3) * N1 + b3], w[g3], acc));
+              const int q = q1 + 2 * q2 + 4 * q3, b = b1 + N1 * b2 + N2 * b3;
+              const int lq = NPE + q, pq = nd[lq], nb = nd[b];
+              const uint16_t tqb = tab[lq * NR + b], tbq = tab[b * NR + lq];
+              const double kv = hd(acc);
+              const size_t p1 = (size_t)P.cp_row_ptr[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (tqb & 0x7fff);
+              if (tqb & 0x8000)
+                P.vals[p1] = kv;
+              else
+                atomicAdd(&P.vals[p1], kv);
+              const size_t p2 = (size_t)P.cp_row_ptr[(size_t)n * nu + nb] + (tbq & 0x7fff);
+              if (tbq & 0x8000)
+                P.vals[p2] = kv;
+              else
+                atomicAdd(&P.vals[p2], kv);
+            }
         }
       }
       // structurally zero pressure-pressure entries, stored by their first contributor
