@@ -47,6 +47,21 @@ class FEMeshDesc(C.Structure):
     ]
 
 
+class FENewtonOptions(C.Structure):
+    _fields_ = [
+        ("max_iterations", C.c_int32), ("atol", C.c_double), ("alpha", C.c_double), ("max_step", C.c_double),
+        ("min_lambda", C.c_double), ("ksp_rtol", C.c_double), ("ksp_restart", C.c_int32),
+        ("ksp_max_iterations", C.c_int32), ("forcing", C.c_int32),
+    ]
+
+
+class FENewtonReport(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int32), ("converged", C.c_int32), ("linear_iterations", C.c_int64),
+        ("residual_norm_initial", C.c_double), ("residual_norm", C.c_double), ("last_lambda", C.c_double),
+    ]
+
+
 # Every symbol include/cm_fe.h declares, with its argument types.
 _vp, _i32, _i64 = C.c_void_p, C.c_int32, C.c_int64
 SIGNATURES = {
@@ -67,6 +82,8 @@ SIGNATURES = {
     "fe_set_high_precision": [_vp, _i32],
     "fe_set_surface_pressure": [_vp, _vp],
     "fe_set_materials": [_vp, _vp],
+    "fe_newton_options_default": [C.POINTER(FENewtonOptions)],
+    "fe_newton_load_step": [_vp, _vp, _vp, _i64, _vp, C.POINTER(FENewtonOptions), C.POINTER(FENewtonReport), _vp],
     "fe_check": [_vp, _vp],
     "fe_launch_count": [_vp, C.POINTER(_i64)],
     "fe_last_error": [C.c_char_p, _i32],
@@ -91,6 +108,9 @@ SIGNATURES = {
     "ws_mlp_forward_bf16": [_i32, _i32, _vp, _vp, _vp, _vp, _vp, _i32, _vp],
 }
 
+# Functions of the C ABI that return nothing.
+VOID_FUNCTIONS = {"fe_newton_options_default"}
+
 WS_ACT_IDENTITY = 0
 WS_ACT_TANH = 1
 
@@ -111,7 +131,7 @@ def load(path: str | None = None):
     for name, args in SIGNATURES.items():
         f = getattr(L, name)
         f.argtypes = args
-        f.restype = C.c_int
+        f.restype = None if name in VOID_FUNCTIONS else C.c_int
     _lib = L
     return L
 

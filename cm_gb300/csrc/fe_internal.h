@@ -147,6 +147,11 @@ int launch_mixed_batch(int variant, unsigned mask, const BatchMember* members, i
 int launch_batch_typed(int variant, int type, unsigned mask, const BatchMember* members, int n, const BatchArgs& a,
                        int ctas_per_sm, int num_sms, void* stream);
 
+// Device CSR pattern (0-based row pointers and columns) and sizes of a handle
+// (fe_kernels.cu), for the Newton driver (fe_newton.cu).
+int device_pattern(fe_handle h, const int32_t** row_ptr, const int32_t** col, int64_t* ndofs, int64_t* nnz,
+                   int64_t* nu3);
+
 // Records the text fe_last_error() returns (per calling thread) and returns code.
 int record_error(int code, const std::string& msg);
 

@@ -479,6 +479,7 @@ struct fe_equations_set {
   bool has_surfp = false;
   int high_precision = FE_HIGH_PRECISION_FP64;
   unsigned* d_status = nullptr;
+  int32_t* d_col = nullptr;  // CSR columns on the device, uploaded on first use (Newton driver)
   // staging for calls given host memory
   double *s_x = nullptr, *s_r = nullptr, *s_vals = nullptr, *s_cp = nullptr, *s_elem = nullptr;
   float* s_uu = nullptr;
@@ -797,6 +798,22 @@ int noalloc_scratch(int device, double** out) {
 
 namespace cmfe {
 int record_error(int code, const std::string& msg) { return set_error(code, msg); }
+
+int device_pattern(fe_handle h, const int32_t** row_ptr, const int32_t** col, int64_t* ndofs, int64_t* nnz,
+                   int64_t* nu3) {
+  if (!h) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL handle");
+  std::lock_guard<std::mutex> lk(h->mu);
+  if (!h->d_col) {
+    CUDA_TRY(cudaMalloc(&h->d_col, sizeof(int32_t) * h->hs.col.size()));
+    CUDA_TRY(cudaMemcpy(h->d_col, h->hs.col.data(), sizeof(int32_t) * h->hs.col.size(), cudaMemcpyHostToDevice));
+  }
+  *row_ptr = h->d_row_ptr;
+  *col = h->d_col;
+  *ndofs = h->hs.ndofs;
+  *nnz = h->hs.nnz;
+  *nu3 = 3 * (int64_t)h->hs.nu;
+  return FE_NO_ERROR;
+}
 }  // namespace cmfe
 
 extern "C" {
@@ -857,7 +874,7 @@ int fe_destroy(fe_handle h) {
   void* ptrs[] = {h->d_surfp, h->d_bnd_elems, h->d_bnd_mask, h->d_geo_dd, h->d_elem_u, h->d_elem_p, h->d_row_ptr, h->d_uu_row_ptr, h->d_cp_row_ptr, h->d_wu,
                   h->d_wp, h->d_elem_table, h->d_colour_elems, h->d_tables, h->d_geo, h->d_mat,
                   h->d_gbf_u, h->d_gbf_p, h->d_gw, h->d_status, h->s_x, h->s_r, h->s_vals, h->s_cp,
-                  h->s_uu, h->s_elem};
+                  h->s_uu, h->s_elem, h->d_col};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete h;

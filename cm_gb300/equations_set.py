@@ -222,6 +222,29 @@ class FiniteElasticityEquationsSet:
         check(_lib.load().fe_set_high_precision(self._h, code))
         self.high_precision = mode
 
+    def newton_load_step(self, x, fixed_dofs, fixed_values, **options):
+        """fe_newton_load_step: one load increment by Newton on the device
+        (FP64 Jacobian, block-diagonal-preconditioned GMRES, cubic
+        backtracking).  x (numpy array or CUDA tensor of all dofs) is the
+        initial guess and receives the converged state; fixed_dofs take
+        fixed_values.  Options are the fields of fe_newton_options
+        (max_iterations, atol, alpha, max_step, min_lambda, ksp_rtol,
+        ksp_restart, ksp_max_iterations, forcing).  Returns the report as a
+        dict."""
+        L = _lib.load()
+        o = _lib.FENewtonOptions()
+        L.fe_newton_options_default(C.byref(o))
+        for k, v in options.items():
+            if not hasattr(o, k):
+                raise ValueError("unknown Newton option " + k)
+            setattr(o, k, v)
+        dofs = np.ascontiguousarray(fixed_dofs, dtype=np.int32)
+        vals = np.ascontiguousarray(np.broadcast_to(np.asarray(fixed_values, dtype=np.float64), dofs.shape))
+        rep = _lib.FENewtonReport()
+        check(L.fe_newton_load_step(self._h, dofs.ctypes.data, vals.ctypes.data, int(dofs.size), _ptr(x),
+                                    C.byref(o), C.byref(rep), _stream(x)))
+        return {k: getattr(rep, k) for k, _ in rep._fields_}
+
     def check_status(self, x=None):
         check(_lib.load().fe_check(self._h, _stream(x)))
 

@@ -256,6 +256,52 @@ int fe_batch_launch_count(fe_batch b, int64_t* count);
 #define FE_NOALLOC_MAX_DOFS 1048576
 int fe_residual_evaluate_noalloc(fe_handle h, const double* x, double* r, void* stream);
 
+/* ---- Newton load step (replaces the SNES solve the reference runs around the
+ * assembly: SOLVER_NEWTON_LINESEARCH defaults, solver_routines.f90:17803-17812,
+ * line search :18772-18775, tolerances :18674; Dirichlet rows and columns
+ * dropped from the linear system as the solver mapping does,
+ * solver_mapping_routines.f90:1420,1592).
+ *
+ * One load increment: the fixed dofs take fixed_values (the caller applies
+ * the increment rule NEW = CUR + (FULL - CUR)/(N - i + 1) of
+ * equations_set_routines.f90:6568-6590 to form them); x, in: the initial
+ * guess (the reference's: the current field), out: the converged state.
+ * Newton with the FP64 Jacobian (fe_jacobian_evaluate), stopping when
+ * ||r_free||_2 <= atol or after max_iterations; each step solves the Newton
+ * system by right-preconditioned restarted GMRES (classical Gram-Schmidt
+ * with one re-orthogonalisation) with a block-diagonal preconditioner
+ * (Jacobi on displacement rows, the inverse of diag(B diag(A)^-1 B^T) on
+ * pressure rows), then takes a cubic backtracking line search on
+ * 1/2 ||r_free||^2 (sufficient decrease alpha, step cap max_step); a trial
+ * state with det F <= 0 counts as a failed trial step.  Everything runs on
+ * the device; x may be host or device memory.  Returns FE_ERR_NUMERICAL when
+ * the initial state already has an inverted element, FE_NO_ERROR otherwise
+ * (convergence is in the report). */
+typedef struct fe_newton_options {
+  int32_t max_iterations;     /* 50 */
+  double atol;                /* 1e-10 on ||r_free||_2 */
+  double alpha;               /* 1e-4, line-search sufficient decrease */
+  double max_step;            /* 1e8, cap on ||dx||_2 */
+  double min_lambda;          /* 1e-10, smallest line-search step */
+  double ksp_rtol;            /* 1e-5, GMRES relative tolerance (reference KSP default) */
+  int32_t ksp_restart;        /* 30 */
+  int32_t ksp_max_iterations; /* 600 per Newton step */
+  int32_t forcing;            /* 0: fixed ksp_rtol; 1: Eisenstat-Walker choice 2 */
+} fe_newton_options;
+
+typedef struct fe_newton_report {
+  int32_t iterations;         /* Newton iterations taken */
+  int32_t converged;          /* 1 when ||r_free||_2 <= atol */
+  int64_t linear_iterations;  /* GMRES iterations over all Newton steps */
+  double residual_norm_initial;
+  double residual_norm;       /* final ||r_free||_2 */
+  double last_lambda;         /* step length of the last line search */
+} fe_newton_report;
+
+void fe_newton_options_default(fe_newton_options* options);
+int fe_newton_load_step(fe_handle h, const int32_t* fixed_dofs, const double* fixed_values, int64_t num_fixed,
+                        double* x, const fe_newton_options* options, fe_newton_report* report, void* stream);
+
 /* Waits for the handle's work on `stream` and reports numerical problems
  * seen by the kernels since the last call (FE_ERR_NUMERICAL) — the device
  * counterpart of the reference's error flags, set instead of trapping. */

@@ -282,3 +282,69 @@ def test_gpu_guccione_slab_matches_oracle_newton(cuda, oracle):
         if prec == "fp64":
             assert [r.iterations for r in rg] == [r.iterations for r in ro]
         assert float((xg.cpu() - xo).abs().max()) < 1e-9
+
+
+# ------------------------------------------- native Newton (fe_newton_load_step)
+def native_solve(m, bc, increments, on_device=True, **opt):
+    """Load increments through the C ABI's Newton load step, the caller
+    applying the reference's increment rule to the Dirichlet values."""
+    from cm_gb300 import FiniteElasticityEquationsSet
+    es = FiniteElasticityEquationsSet(m)
+    x = N.initial_state(m)
+    reports = []
+    for i in range(1, increments + 1):
+        cur = x[bc.dofs]
+        new = bc.full.copy() if i == increments else \
+            np.where(bc.incremented, cur + (bc.full - cur) / (increments - i + 1), bc.full)
+        if on_device:
+            xd = torch.from_numpy(x).cuda()
+            rep = es.newton_load_step(xd, bc.dofs, new, **opt)
+            x = xd.cpu().numpy()
+        else:
+            rep = es.newton_load_step(x, bc.dofs, new, **opt)
+        reports.append(rep)
+    return x, reports
+
+
+@pytest.mark.gpu
+def test_native_newton_matches_oracle_config1(cuda, oracle):
+    """fe_newton_load_step on the 4x4x4 trilinear cube (element pressure),
+    5 increments: converges at every increment to the oracle's solution."""
+    m = cube_cfg1()
+    bc = N.uniaxial_symmetry_conditions(m, 1.1)
+    xo, ro = oracle_solve(oracle, m, bc, 5, linear="dense")
+    xn, rn = native_solve(m, bc, 5, ksp_rtol=1e-10, ksp_max_iterations=2000)
+    for a, b in zip(rn, ro):
+        assert a["converged"] == 1 and a["residual_norm"] <= 1e-10
+        assert a["iterations"] <= b.iterations + 1
+    assert float(np.abs(xn - xo.numpy()).max()) < 1e-9
+
+
+@pytest.mark.gpu
+def test_native_newton_matches_oracle_triquadratic(cuda, oracle):
+    """Triquadratic / nodal pressure, clamped stretch and shear, 2 increments:
+    the native load step reaches ||r_free||_2 <= 1e-10 and the oracle's
+    solution; host and device state buffers give bit-identical results."""
+    m = quad_small()
+    bc = N.clamped_stretch_shear_conditions(m, 1.15, 0.05)
+    xo, ro = oracle_solve(oracle, m, bc, 2, linear="dense")
+    xn, rn = native_solve(m, bc, 2, ksp_rtol=1e-8)
+    assert all(r["converged"] == 1 and r["residual_norm"] <= 1e-10 for r in rn)
+    assert all(r["linear_iterations"] > 0 for r in rn)
+    assert float(np.abs(xn - xo.numpy()).max()) < 1e-9
+    xh, rh = native_solve(m, bc, 2, on_device=False, ksp_rtol=1e-8)
+    assert np.array_equal(xh, xn)
+    assert [r["iterations"] for r in rh] == [r["iterations"] for r in rn]
+
+
+@pytest.mark.gpu
+def test_native_newton_rejects_inverted_initial_state(cuda):
+    from cm_gb300 import FEError, FiniteElasticityEquationsSet
+    m = quad_small()
+    es = FiniteElasticityEquationsSet(m)
+    x = N.initial_state(m)
+    x[:m.nu] *= -1.0  # mirror x: every element inverted
+    bc = N.clamped_stretch_shear_conditions(m, 1.1, 0.0)
+    with pytest.raises(FEError) as e:
+        es.newton_load_step(x, bc.dofs, x[bc.dofs])
+    assert e.value.code == -5
