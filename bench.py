@@ -176,7 +176,25 @@ def cpu_baseline(m, x, rp1, col1, budget_s=12.0):
     dt = time.perf_counter() - t0
     return {"value": n * m.ne / dt, "unit": UNIT, "cores": nt, "kind": "port",
             "sample": "%d full assemblies (Jacobian+residual, FP64) of the benchmark mesh, %d threads, %.1f s" % (
-                n, nt, dt)}
+                n, nt, dt)}, vals, res
+
+
+def error_vs_oracle(es, mixed, vals_gpu, vc_gpu, r_gpu, vals_or, r_or):
+    """Largest difference of the GPU assembly from the FP64 oracle's assembly
+    of the same state, relative to the largest magnitude of each block."""
+    import numpy as np
+
+    def rel(a, b):
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+    out = {"reference": "FP64 oracle, whole assembly of the same state", "residual": rel(r_gpu, r_or)}
+    if mixed:
+        from cm_gb300.newton import mixed_positions
+        uu_pos, cp_pos = mixed_positions(es)
+        out["uu_block_fp32"] = rel(vals_gpu.astype(np.float64), vals_or[uu_pos])
+        out["coupling_blocks"] = rel(vc_gpu, vals_or[cp_pos])
+    else:
+        out["jacobian"] = rel(vals_gpu, vals_or)
+    return out
 
 
 def reference_arm(args):
@@ -401,7 +419,9 @@ def our_arm(args):
         out["mixed_double_float"] = dfloat
     if world == 1 and not args.no_cpu:
         rp1, col1 = es.csr_pattern(base=1)
-        out["cpu_baseline"] = cpu_baseline(m, x, rp1, col1)
+        out["cpu_baseline"], vals_or, r_or = cpu_baseline(m, x, rp1, col1)
+        out["error_vs_oracle"] = error_vs_oracle(es, mixed, vuh if mixed else vh, vch if mixed else None, rh,
+                                                 vals_or, r_or)
     if world == 1 and args.loadstep:
         del es, r, xd
         torch.cuda.empty_cache()

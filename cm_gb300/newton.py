@@ -208,6 +208,23 @@ def _gmres(A, b, M, rtol, restart, max_it, check_every=6):
     return x, total
 
 
+def mixed_positions(es):
+    """Positions in the full CSR pattern (0-based) of the entries of the
+    mixed split (fe_mixed_layout): each displacement row holds its uu
+    entries first, then its coupling entries; pressure rows hold coupling
+    entries only."""
+    uu_rp, cp_rp = (a.astype(np.int64) for a in es.mixed_layout())
+    rp = es.csr_pattern()[0].astype(np.int64)
+    nu3 = 3 * es.mesh.nu
+    ku = np.zeros(es.ndofs, dtype=np.int64)
+    ku[:nu3] = np.diff(uu_rp)
+    ru = np.repeat(np.arange(nu3), ku[:nu3])
+    uu_pos = rp[ru] + (np.arange(uu_rp[-1]) - uu_rp[ru])
+    rc = np.repeat(np.arange(es.ndofs), np.diff(cp_rp))
+    cp_pos = rp[rc] + ku[rc] + (np.arange(cp_rp[-1]) - cp_rp[rc])
+    return uu_pos, cp_pos
+
+
 class LoadStepSolver:
     """Load-stepped Newton for one equations set on the GPU."""
 
@@ -221,17 +238,7 @@ class LoadStepSolver:
         self.bc_dofs = torch.from_numpy(bc.dofs).to(self.device)
         if self.opt.precision == "mixed":
             es.set_high_precision(self.opt.high_precision)
-            uu_rp, cp_rp = (a.astype(np.int64) for a in es.mixed_layout())
-            rp = es.csr_pattern()[0].astype(np.int64)
-            nu3 = 3 * es.mesh.nu
-            # positions of the mixed split's entries in the full pattern: each
-            # displacement row holds its uu entries first, then its coupling entries
-            ku = np.zeros(es.ndofs, dtype=np.int64)
-            ku[:nu3] = np.diff(uu_rp)
-            ru = np.repeat(np.arange(nu3), ku[:nu3])
-            uu_pos = rp[ru] + (np.arange(uu_rp[-1]) - uu_rp[ru])
-            rc = np.repeat(np.arange(es.ndofs), np.diff(cp_rp))
-            cp_pos = rp[rc] + ku[rc] + (np.arange(cp_rp[-1]) - cp_rp[rc])
+            uu_pos, cp_pos = mixed_positions(es)
             self.uu_pos = torch.from_numpy(uu_pos).to(self.device)
             self.cp_pos = torch.from_numpy(cp_pos).to(self.device)
             self.vu = torch.empty(es.nnz_uu, dtype=torch.float32, device=self.device)
