@@ -1314,6 +1314,9 @@ int fe_batch_autotune(fe_batch b, const double* const* x, float* const* values_u
   cudaEvent_t e0, e1;
   CUDA_TRY(cudaEventCreate(&e0));
   CUDA_TRY(cudaEventCreate(&e1));
+  int smem_per_sm = 0, smem_reserved = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, b->device));
+  CUDA_TRY(cudaDeviceGetAttribute(&smem_reserved, cudaDevAttrReservedSharedMemoryPerBlock, b->device));
   const int keep_v = b->variant, keep_c = b->ctas_per_sm, keep_b = b->block_groups;
   double best = 1e300;
   int bv = keep_v, bc = keep_c, bb = keep_b;
@@ -1321,7 +1324,7 @@ int fe_batch_autotune(fe_batch b, const double* const* x, float* const* values_u
   for (int v = 0; v < cmfe::batch_variants() && !rc; ++v)
     for (int cps = 1; cps <= 3 && !rc; ++cps) {
       // skip a CTA count the shared memory cannot hold (the launch would use fewer)
-      if (cps * (cmfe::batch_smem(v, b->type_mask) + 1024) > 232448) continue;
+      if (cps * (cmfe::batch_smem(v, b->type_mask) + smem_reserved) > smem_per_sm) continue;
       for (int bg : blocks) {
         b->variant = v;
         b->ctas_per_sm = cps;

@@ -69,7 +69,7 @@ struct MixCfg {
   static constexpr int BROWS = NT * 8;
   static constexpr int REC64 = 20;  // P(9), A(9), t1, pad
   static constexpr int REC32 = 60;  // D^{mn}(k,l) for 6 blocks, padded so Gauss points 2 apart hit banks 24 apart
-  static constexpr int PHS = 84;    // per-Gauss-point stride of the FP32 gradient table (conflict-free fragment loads)
+  static constexpr int PHS = 4 * NPE;  // per-Gauss-point stride of the FP32 gradient table: [b][d0, d1, d2, 0]
   static constexpr int KAP = 84;    // contraction length: kappa = 28 k + g, g < 27 (g = 27 is padding)
   static constexpr int O_PSI64 = 0;
   static constexpr int O_L = align16(O_PSI64 + NG * 8 * 8);
@@ -235,7 +235,7 @@ __device__ __forceinline__ void mix_tables(const KParams& P, unsigned char* sm) 
   H* s_dz = reinterpret_cast<H*>(sm + C::O_DZ);      // [el][g][c*3+k]
   H* s_pg = reinterpret_cast<H*>(sm + C::O_PG);      // [el][g]
   H* s_r64 = reinterpret_cast<H*>(sm + C::O_R64);    // [el][g][REC64]
-  float* s_phi32 = reinterpret_cast<float*>(sm + C::O_PHI32);  // [g][l][b]
+  float* s_phi32 = reinterpret_cast<float*>(sm + C::O_PHI32);  // [g][b][l], l padded to 4
   float* s_r32 = reinterpret_cast<float*>(sm + C::O_R32);      // [el][g][REC32]
   uint32_t* s_A = reinterpret_cast<uint32_t*>(sm + C::O_A);    // [hi/lo][a][KPW]
   float* s_f32 = reinterpret_cast<float*>(sm + C::O_F32);      // scratch of P3 and P4 (EG x 2592 B)
@@ -266,7 +266,8 @@ __device__ __forceinline__ void mix_tables(const KParams& P, unsigned char* sm) 
   }
   for (int i = tid; i < NG * 3 * NPE; i += C::THREADS) {
     const int g = i / (3 * NPE), l = (i / NPE) % 3, b = i % NPE;
-    s_phi32[g * C::PHS + l * NPE + b] = (float)P.gbf_u[(g * 4 + l + 1) * NPE + b];
+    s_phi32[g * C::PHS + 4 * b + l] = (float)P.gbf_u[(g * 4 + l + 1) * NPE + b];
+    if (l == 0) s_phi32[g * C::PHS + 4 * b + 3] = 0.0f;
   }
   for (int i = tid; i < C::AROWS * KPW; i += C::THREADS) {
     const int a = i / KPW, wd = i % KPW;
@@ -304,7 +305,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
   H* s_dz = reinterpret_cast<H*>(sm + C::O_DZ);      // [el][g][c*3+k]
   H* s_pg = reinterpret_cast<H*>(sm + C::O_PG);      // [el][g]
   H* s_r64 = reinterpret_cast<H*>(sm + C::O_R64);    // [el][g][REC64]
-  float* s_phi32 = reinterpret_cast<float*>(sm + C::O_PHI32);  // [g][l][b]
+  float* s_phi32 = reinterpret_cast<float*>(sm + C::O_PHI32);  // [g][b][l], l padded to 4
   float* s_r32 = reinterpret_cast<float*>(sm + C::O_R32);      // [el][g][REC32]
   uint32_t* s_A = reinterpret_cast<uint32_t*>(sm + C::O_A);    // [hi/lo][a][KPW]
   float* s_f32 = reinterpret_cast<float*>(sm + C::O_F32);      // scratch of P3 and P4 (EG x 2592 B)
@@ -775,13 +776,13 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
               float w0 = 0.f, w1 = 0.f;
               if (kv && v0) {
                 const float* dt = &r32[g * C::REC32 + blk0 * 9 + k * 3];
-                const float* ph = &s_phi32[g * C::PHS + b0];
-                w0 = dt[0] * ph[0] + dt[1] * ph[NPE] + dt[2] * ph[2 * NPE];
+                const float4 ph = *reinterpret_cast<const float4*>(&s_phi32[g * C::PHS + 4 * b0]);
+                w0 = dt[0] * ph.x + dt[1] * ph.y + dt[2] * ph.z;
               }
               if (kv && v1) {
                 const float* dt = &r32[g * C::REC32 + blk1 * 9 + k * 3];
-                const float* ph = &s_phi32[g * C::PHS + b1];
-                w1 = dt[0] * ph[0] + dt[1] * ph[NPE] + dt[2] * ph[2 * NPE];
+                const float4 ph = *reinterpret_cast<const float4*>(&s_phi32[g * C::PHS + 4 * b1]);
+                w1 = dt[0] * ph.x + dt[1] * ph.y + dt[2] * ph.z;
               }
               wv[0][j] = w0;
               wv[1][j] = w1;
