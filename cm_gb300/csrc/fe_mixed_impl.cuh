@@ -730,7 +730,11 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
       // A fragments (W values) in registers from the per-Gauss-point D^{blk}
       // records and the gradient table, and takes B = Phi from shared memory.
       if (!P.res_only) {
-        constexpr int MROWS = 6 * NPE;
+        // Rows of the stacked blocks: block blk occupies rows [blk * BS, blk * BS + NPE).
+        // For triquadratic elements BS = 32, so that a 16-row tile never spans
+        // two blocks and the two rows a thread holds share the D^{blk} loads.
+        constexpr int BS = NPE > 16 ? 32 : NPE;
+        constexpr int MROWS = 6 * BS;
         constexpr int MT2 = (MROWS + 15) / 16;
         const int gq = lane >> 2, tq = lane & 3;
         const uint32_t* Bhi = s_A;
@@ -763,8 +767,8 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
 #pragma unroll
             for (int h = 0; h < 4; ++h) acc[nt][h] = 0.f;
           const int R0 = 16 * mt + gq, R1 = R0 + 8;
-          const int blk0 = R0 / NPE, b0 = R0 % NPE, blk1 = R1 / NPE, b1 = R1 % NPE;
-          const bool v0 = R0 < MROWS, v1 = R1 < MROWS;
+          const int blk0 = R0 / BS, b0 = R0 % BS, blk1 = R1 / BS, b1 = R1 % BS;
+          const bool v0 = R0 < MROWS && b0 < NPE, v1 = R1 < MROWS && b1 < NPE;
 #pragma unroll 1
           for (int kt = 0; kt < C::KT; ++kt) {
             float wv[2][4];  // [row r0/r1][kappa 2t, 2t+1, 2t+8, 2t+9]
@@ -774,15 +778,30 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
               const int k = kap / 28, g = kap % 28;
               const bool kv = kap < C::KAP && g < NG;
               float w0 = 0.f, w1 = 0.f;
-              if (kv && v0) {
-                const float* dt = &r32[g * C::REC32 + blk0 * 9 + k * 3];
-                const float4 ph = *reinterpret_cast<const float4*>(&s_phi32[g * C::PHS + 4 * b0]);
-                w0 = dt[0] * ph.x + dt[1] * ph.y + dt[2] * ph.z;
-              }
-              if (kv && v1) {
-                const float* dt = &r32[g * C::REC32 + blk1 * 9 + k * 3];
-                const float4 ph = *reinterpret_cast<const float4*>(&s_phi32[g * C::PHS + 4 * b1]);
-                w1 = dt[0] * ph.x + dt[1] * ph.y + dt[2] * ph.z;
+              if constexpr (BS % 16 == 0) {  // both rows in block blk0
+                if (kv && (v0 || v1)) {
+                  const float* dt = &r32[g * C::REC32 + blk0 * 9 + k * 3];
+                  const float d0 = dt[0], d1 = dt[1], d2 = dt[2];
+                  if (v0) {
+                    const float4 ph = *reinterpret_cast<const float4*>(&s_phi32[g * C::PHS + 4 * b0]);
+                    w0 = d0 * ph.x + d1 * ph.y + d2 * ph.z;
+                  }
+                  if (v1) {
+                    const float4 ph = *reinterpret_cast<const float4*>(&s_phi32[g * C::PHS + 4 * b1]);
+                    w1 = d0 * ph.x + d1 * ph.y + d2 * ph.z;
+                  }
+                }
+              } else {
+                if (kv && v0) {
+                  const float* dt = &r32[g * C::REC32 + blk0 * 9 + k * 3];
+                  const float4 ph = *reinterpret_cast<const float4*>(&s_phi32[g * C::PHS + 4 * b0]);
+                  w0 = dt[0] * ph.x + dt[1] * ph.y + dt[2] * ph.z;
+                }
+                if (kv && v1) {
+                  const float* dt = &r32[g * C::REC32 + blk1 * 9 + k * 3];
+                  const float4 ph = *reinterpret_cast<const float4*>(&s_phi32[g * C::PHS + 4 * b1]);
+                  w1 = dt[0] * ph.x + dt[1] * ph.y + dt[2] * ph.z;
+                }
               }
               wv[0][j] = w0;
               wv[1][j] = w1;
