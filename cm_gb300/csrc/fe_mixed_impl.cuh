@@ -113,6 +113,16 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
+// Four 8x8 b16 matrices from shared memory (ldmatrix, not transposed): lane L
+// gives the address of row L % 8 of matrix L / 8 (16-byte aligned); register i
+// receives the thread's element pair of matrix i (row lane / 4, pair lane % 4).
+__device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], const void* row_addr) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(row_addr);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+
 // Block (m, n) of the lower-triangle displacement blocks: 0..2 diagonal,
 // 3 = (1,0), 4 = (2,0), 5 = (2,1).
 __device__ __forceinline__ void blk_mn(int blk, int& m, int& n) {
@@ -813,12 +823,15 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
             split_bf16(wv[1][2], wv[1][3], ah[3], al[3]);  // row r1, cols 2t+8..
 #pragma unroll
             for (int nt = 0; nt < C::NT; ++nt) {
-              const int rb = (8 * nt + gq) * KPW, c0 = 8 * kt + tq, c1 = c0 + 4;
-              const uint32_t bh0 = Bhi[rb + c0], bh1 = Bhi[rb + c1];
-              mma_bf16(acc[nt], ah[0], ah[1], ah[2], ah[3], bh0, bh1);
+              // B fragments of this n-tile: high and low parts, kappa halves
+              // 16 kt .. 16 kt + 7 and 16 kt + 8 .. 16 kt + 15, in one ldmatrix
+              const int mi = lane >> 3;
+              uint32_t bf[4];
+              ldmatrix_x4(bf, (mi < 2 ? Bhi : Blo) + (8 * nt + (lane & 7)) * KPW + 8 * kt + 4 * (mi & 1));
+              mma_bf16(acc[nt], ah[0], ah[1], ah[2], ah[3], bf[0], bf[1]);
               if (SPLIT == 3) {
-                mma_bf16(acc[nt], ah[0], ah[1], ah[2], ah[3], Blo[rb + c0], Blo[rb + c1]);
-                mma_bf16(acc[nt], al[0], al[1], al[2], al[3], bh0, bh1);
+                mma_bf16(acc[nt], ah[0], ah[1], ah[2], ah[3], bf[2], bf[3]);
+                mma_bf16(acc[nt], al[0], al[1], al[2], al[3], bf[0], bf[1]);
               }
             }
           }
