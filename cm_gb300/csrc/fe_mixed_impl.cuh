@@ -232,26 +232,16 @@ __device__ __forceinline__ void lagrange_1d(int a, double t, double& bv, double&
 template <int N1, int PM, int EG_, class H>
 __device__ __forceinline__ void mix_tables(const KParams& P, unsigned char* sm) {
   using C = MixCfg<N1, PM, EG_>;
-  constexpr int NPE = C::NPE, NPP = C::NPP, NR = C::NR, NU3 = C::NU3, NROW = C::NROW, EG = C::EG;
-  constexpr int KPW = C::KPW;
+  constexpr int NPE = C::NPE, KPW = C::KPW;
   H* s_psi = reinterpret_cast<H*>(sm + C::O_PSI64);  // [g][q]
   H* s_L = reinterpret_cast<H*>(sm + C::O_L);        // [q][gi]
   H* s_w = reinterpret_cast<H*>(sm + C::O_W);        // [g]
   H* s_B1 = reinterpret_cast<H*>(sm + C::O_1D);      // [gi][a] 1-D values
   H* s_D1 = s_B1 + 3 * N1;                                // [gi][a] 1-D derivatives
   H* s_LM = reinterpret_cast<H*>(sm + C::O_LM);      // [B|D][q][gi][a]: L(q, gi) x 1-D value | derivative
-  H* s_z = reinterpret_cast<H*>(sm + C::O_Z);        // [el][c][a]
-  H* s_p = reinterpret_cast<H*>(sm + C::O_P);        // [el][q]
-  H* s_dz = reinterpret_cast<H*>(sm + C::O_DZ);      // [el][g][c*3+k]
-  H* s_pg = reinterpret_cast<H*>(sm + C::O_PG);      // [el][g]
-  H* s_r64 = reinterpret_cast<H*>(sm + C::O_R64);    // [el][g][REC64]
   float* s_phi32 = reinterpret_cast<float*>(sm + C::O_PHI32);  // [g][b][l], l padded to 4
-  float* s_r32 = reinterpret_cast<float*>(sm + C::O_R32);      // [el][g][REC32]
   uint32_t* s_A = reinterpret_cast<uint32_t*>(sm + C::O_A);    // [hi/lo][a][KPW]
-  float* s_f32 = reinterpret_cast<float*>(sm + C::O_F32);      // scratch of P3 and P4 (EG x 2592 B)
-  int* s_node = reinterpret_cast<int*>(sm + C::O_NODE);        // [el][NR+1]
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nu = P.nu;
+  const int tid = threadIdx.x;
   // ---- constant tables
   for (int i = tid; i < NG * 8; i += C::THREADS) s_psi[i] = hval<H>(P.gbf_p[i]);
   for (int i = tid; i < NG; i += C::THREADS) s_w[i] = hval<H>(P.gw[i]);
