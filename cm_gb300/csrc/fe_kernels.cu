@@ -506,6 +506,7 @@ struct fe_batch_s {
   double tuned_ms = -1.0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
+  int64_t graph_kernels = 0;  // kernels in the captured graph
   int64_t launches = 0;
   std::mutex mu;
 };
@@ -596,6 +597,33 @@ int run_colours(fe_handle h, KParams kp, cudaStream_t st) {
     int rc = launch<MODE>(h, kp, st);
     if (rc) return rc;
     if ((rc = surface_after(h, kp, c, MODE == M_JAC, st))) return rc;
+  }
+  return FE_NO_ERROR;
+}
+
+// The mixed assembly of one equations set into device buffers: one launch
+// per colour, each followed by that colour's surface-pressure faces.  Adds
+// the number of kernels launched to *count when count is set.
+int mixed_colours(fe_handle h, const double* dx, float* du, double* dc, double* dr, bool double_float,
+                  cudaStream_t st, int64_t* count) {
+  KParams kp = base_params(h);
+  kp.x = dx;
+  kp.vals_uu = du;
+  kp.vals = dc;
+  kp.r = dr;
+  for (int c = 0; c < h->hs.ncolours; ++c) {
+    kp.elems = h->d_colour_elems + h->hs.colour_ptr[c];
+    kp.count = h->hs.colour_ptr[c + 1] - h->hs.colour_ptr[c];
+    const int e = cmfe::launch_mixed(h->hs, kp, h->num_sms, st, double_float);
+    if (e != 0) return set_error(FE_ERR_CUDA, std::string("mixed kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+    if (kp.count > 0) {
+      h->launches++;
+      if (count) ++*count;
+    }
+    const int64_t before = h->launches;
+    int rc = surface_after(h, kp, c, 1, st);
+    if (rc) return rc;
+    if (count) *count += h->launches - before;
   }
   return FE_NO_ERROR;
 }
@@ -735,6 +763,17 @@ int sync_table(fe_batch b, cudaStream_t st) {
 // One batched launch on st; table is the device copy of the member table the
 // launch copies into constant memory.
 int batch_launch_from(fe_batch b, const cmfe::BatchMember* table, cudaStream_t st) {
+  if (b->variant == cmfe::batch_variants()) {
+    // one launch per member and colour: the single-set kernels, in member order
+    for (size_t s = 0; s < b->members.size(); ++s) {
+      const KParams& k = b->h_table[s].kp;
+      fe_handle h = b->members[b->slot_member[s]];
+      std::lock_guard<std::mutex> lk(h->mu);
+      const int rc = mixed_colours(h, k.x, k.vals_uu, k.vals, k.r, false, st, &b->launches);
+      if (rc) return rc;
+    }
+    return FE_NO_ERROR;
+  }
   CUDA_TRY(cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned), st));
   cmfe::BatchArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -1057,19 +1096,8 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
     if ((rc = ensure((void**)&h->s_r, sizeof(double) * h->hs.ndofs))) return rc;
     dr = h->s_r;
   }
-  KParams kp = base_params(h);
-  kp.x = dx;
-  kp.vals_uu = du;
-  kp.vals = dc;
-  kp.r = dr;
-  for (int c = 0; c < h->hs.ncolours; ++c) {
-    kp.elems = h->d_colour_elems + h->hs.colour_ptr[c];
-    kp.count = h->hs.colour_ptr[c + 1] - h->hs.colour_ptr[c];
-    const int e = cmfe::launch_mixed(h->hs, kp, h->num_sms, st, h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT);
-    if (e != 0) return set_error(FE_ERR_CUDA, std::string("mixed kernel launch: ") + cudaGetErrorString((cudaError_t)e));
-    h->launches++;
-    if ((rc = surface_after(h, kp, c, 1, st))) return rc;
-  }
+  if ((rc = mixed_colours(h, dx, du, dc, dr, h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT, st, nullptr)))
+    return rc;
   if (hu) CUDA_TRY(cudaMemcpyAsync(values_uu, du, sizeof(float) * h->hs.nnz_uu, cudaMemcpyDeviceToHost, st));
   if (hc) CUDA_TRY(cudaMemcpyAsync(values_coupling, dc, sizeof(double) * h->hs.nnz_cp, cudaMemcpyDeviceToHost, st));
   if (hr) CUDA_TRY(cudaMemcpyAsync(r, dr, sizeof(double) * h->hs.ndofs, cudaMemcpyDeviceToHost, st));
@@ -1284,7 +1312,7 @@ int fe_batch_check(fe_batch b, void* stream) {
 int fe_batch_set_config(fe_batch b, int32_t variant, int32_t ctas_per_sm, int32_t block_groups) {
   int rc = check_batch(b);
   if (rc) return rc;
-  if (variant < 0 || variant >= cmfe::batch_variants() || ctas_per_sm < 1 || ctas_per_sm > 4 || block_groups < 1)
+  if (variant < 0 || variant > cmfe::batch_variants() || ctas_per_sm < 1 || ctas_per_sm > 4 || block_groups < 1)
     return set_error(FE_ERR_INVALID_ARGUMENT, "invalid batch configuration");
   std::lock_guard<std::mutex> lk(b->mu);
   b->variant = variant;
@@ -1321,11 +1349,15 @@ int fe_batch_autotune(fe_batch b, const double* const* x, float* const* values_u
   double best = 1e300;
   int bv = keep_v, bc = keep_c, bb = keep_b;
   const int blocks[] = {1, 2, 4};
-  for (int v = 0; v < cmfe::batch_variants() && !rc; ++v)
+  for (int v = 0; v <= cmfe::batch_variants() && !rc; ++v)
     for (int cps = 1; cps <= 3 && !rc; ++cps) {
+      // the last variant (one launch per member and colour) has no launch shape
+      const bool per_member = v == cmfe::batch_variants();
+      if (per_member && cps > 1) break;
       // skip a CTA count the shared memory cannot hold (the launch would use fewer)
-      if (cps * (cmfe::batch_smem(v, b->type_mask) + smem_reserved) > smem_per_sm) continue;
+      if (!per_member && cps * (cmfe::batch_smem(v, b->type_mask) + smem_reserved) > smem_per_sm) continue;
       for (int bg : blocks) {
+        if (per_member && bg > 1) break;
         b->variant = v;
         b->ctas_per_sm = cps;
         b->block_groups = bg;
@@ -1388,7 +1420,10 @@ int fe_batch_capture(fe_batch b, const double* const* x, float* const* values_uu
   b->graph = nullptr;
   cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
+    const int64_t l0 = b->launches;
     rc = batch_launch_from(b, b->d_table_graph, cs);
+    b->graph_kernels = b->launches - l0;  // counted when the graph runs, not at capture
+    b->launches = l0;
     e = cudaStreamEndCapture(cs, &b->graph);
     if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&b->graph_exec, b->graph, 0);
   }
@@ -1406,7 +1441,7 @@ int fe_batch_replay(fe_batch b, void* stream) {
   std::lock_guard<std::mutex> g(g_batch_mu);
   if ((rc = batch_serialise_begin(b->device, st))) return rc;
   CUDA_TRY(cudaGraphLaunch(b->graph_exec, st));
-  b->launches++;
+  b->launches += b->graph_kernels;
   return batch_serialise_end(b->device, st);
 }
 

@@ -211,8 +211,10 @@ int fe_batch_check(fe_batch b, void* stream);
 
 /* Launch configuration: variant (elements per group for triquadratic /
  * trilinear members: 0 = 4/8, 1 = 4/4, 2 = 2/4, 3 = 2/2, 4 = 3/2 compiled for
- * three CTAs per SM), CTAs per SM, and
- * consecutive element groups per work unit. */
+ * three CTAs per SM; 5 = no persistent launch but the single-set kernels, one
+ * launch per member and colour, which the autotuner picks when the members
+ * are large enough to fill the GPU on their own), CTAs per SM, and
+ * consecutive element groups per work unit (both ignored by variant 5). */
 int fe_batch_set_config(fe_batch b, int32_t variant, int32_t ctas_per_sm, int32_t block_groups);
 int fe_batch_get_config(fe_batch b, int32_t* variant, int32_t* ctas_per_sm, int32_t* block_groups,
                         double* tuned_ms);
@@ -228,6 +230,7 @@ int fe_batch_autotune(fe_batch b, const double* const* x, float* const* values_u
 int fe_batch_capture(fe_batch b, const double* const* x, float* const* values_uu,
                      double* const* values_coupling, double* const* r, void* stream);
 int fe_batch_replay(fe_batch b, void* stream);
+/* Kernels the batch has run (a replay counts the kernels of its graph). */
 int fe_batch_launch_count(fe_batch b, int64_t* count);
 
 /* ---- Residual evaluation that allocates nothing (no counterpart in the
