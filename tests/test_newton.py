@@ -348,3 +348,25 @@ def test_native_newton_rejects_inverted_initial_state(cuda):
     with pytest.raises(FEError) as e:
         es.newton_load_step(x, bc.dofs, x[bc.dofs])
     assert e.value.code == -5
+
+
+@pytest.mark.gpu
+def test_native_newton_slab_with_cavity_pressure(cuda, oracle):
+    """The native load step on the Guccione slab with the bottom-face pressure
+    raised by the reference's pressure-increment rule (the caller sets the
+    surface load of each increment): the oracle's solution at every
+    increment's end state."""
+    from cm_gb300 import FiniteElasticityEquationsSet
+    m = slab_small()
+    bc = N.clamped_lateral_conditions(m)
+    so = N.LoadStepSolver(oracle.EquationsSet(m), bc, N.NewtonOptions(linear="dense"), device="cpu")
+    xo, ro = so.solve(torch.from_numpy(N.initial_state(m)), 4,
+                      pressure=N.PressureIncrements(N.bottom_face_pressure(m, 0.5)))
+    es = FiniteElasticityEquationsSet(m)
+    pinc = N.PressureIncrements(N.bottom_face_pressure(m, 0.5))
+    x = torch.from_numpy(N.initial_state(m)).cuda()
+    for i in range(1, 5):
+        es.set_surface_pressure(pinc.step(i, 4))
+        rep = es.newton_load_step(x, bc.dofs, bc.full, ksp_rtol=1e-10, ksp_max_iterations=3000)
+        assert rep["converged"] == 1 and rep["residual_norm"] <= 1e-10
+    assert float((x.cpu() - xo).abs().max()) < 1e-9
