@@ -136,6 +136,36 @@ template <class H>
 __device__ void mix_stress(int law, const H* c, const H F[3][3], H J, H p, H sig[3][3]) {
   const H s = hrcbrt(J);
   const H zero = hval<H>(0.0), one = hval<H>(1.0), two = hval<H>(2.0), half = hval<H>(0.5);
+  if (law == FE_LAW_MOONEY_RIVLIN) {
+    // S_bar = al I + be C_bar, so F_bar S_bar F_bar^T = al B_bar + be B_bar^2 with
+    // B_bar = F_bar F_bar^T (and tr C_bar = tr B_bar): fewer FP64 operations
+    // than forming C_bar and both products
+    const H s2 = s * s;
+    H Bb[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = i; j < 3; ++j) {
+        Bb[i][j] = s2 * (F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2]);
+        Bb[j][i] = Bb[i][j];
+      }
+    const H I1 = Bb[0][0] + Bb[1][1] + Bb[2][2];
+    const H al = two * (c[0] + I1 * c[1]);
+    const H be = -(two * c[1]);
+    const H rJ = one / J;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = i; j < 3; ++j) {
+        const H b2 = Bb[i][0] * Bb[0][j] + Bb[i][1] * Bb[1][j] + Bb[i][2] * Bb[2][j];
+        sig[i][j] = (al * Bb[i][j] + be * b2) * rJ;
+        sig[j][i] = sig[i][j];
+      }
+    const H tr3 = (sig[0][0] + sig[1][1] + sig[2][2]) * hval<H>(1.0 / 3.0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) sig[i][i] = sig[i][i] - tr3 + p;
+    return;
+  }
   H Fb[3][3], Cb[3][3], S[3][3], T[3][3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
