@@ -174,9 +174,40 @@ def cpu_baseline(m, x, rp1, col1, budget_s=12.0):
         if time.perf_counter() - t0 > budget_s or n >= 20:
             break
     dt = time.perf_counter() - t0
-    return {"value": n * m.ne / dt, "unit": UNIT, "cores": nt, "kind": "port",
+    # one host thread (the reference's serial per-rank loop) on a sample of the mesh
+    n1 = min(m.ne, 2048)
+    t1 = time.perf_counter()
+    if lib.or_assemble_range(P.ref, x.ctypes.data, rp1.ctypes.data, col1.ctypes.data, vals.ctypes.data,
+                             res.ctypes.data, 0, n1, 1) != 0:
+        raise RuntimeError("oracle assembly failed")
+    d1 = time.perf_counter() - t1
+    # vals / res now hold the sampled elements only: assemble the whole mesh again for the error check
+    if lib.or_assemble(P.ref, x.ctypes.data, rp1.ctypes.data, col1.ctypes.data, vals.ctypes.data,
+                       res.ctypes.data, nt) != 0:
+        raise RuntimeError("oracle assembly failed")
+    return {"value": n * m.ne / dt, "unit": UNIT, "cores": nt, "kind": "port", "cpu": host_cpu(),
             "sample": "%d full assemblies (Jacobian+residual, FP64) of the benchmark mesh, %d threads, %.1f s" % (
-                n, nt, dt)}, vals, res
+                n, nt, dt),
+            "single_thread": {"value": n1 / d1, "unit": UNIT, "cores": 1,
+                              "sample": "the first %d elements of the mesh, one thread, %.2f s" % (n1, d1)}}, vals, res
+
+
+def host_cpu():
+    """Model of the host CPU and its thread count, from /proc/cpuinfo."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+                if key == "cpu part" and model is None:
+                    model = "Arm CPU part " + line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return {"model": model or platform.processor() or platform.machine(), "threads": os.cpu_count()}
 
 
 def error_vs_oracle(es, mixed, vals_gpu, vc_gpu, r_gpu, vals_or, r_or):
