@@ -166,17 +166,25 @@ def test_line_search_backtracks_on_a_large_step(oracle):
 def test_mixed_split_positions_cover_the_pattern():
     """Host logic of the mixed path: the uu and coupling positions partition
     the full pattern (checked on the layout arithmetic alone)."""
-    rp = np.array([0, 5, 9, 13, 15])         # 3 u rows (nu = 1) + 1 p row
-    uu_rp = np.array([0, 4, 7, 10])
-    cp_rp = np.array([0, 1, 2, 3, 5])
-    nu3, nd = 3, 4
-    ku = np.zeros(nd, dtype=np.int64)
-    ku[:nu3] = np.diff(uu_rp)
-    ru = np.repeat(np.arange(nu3), ku[:nu3])
-    uu_pos = rp[ru] + (np.arange(uu_rp[-1]) - uu_rp[ru])
-    rc = np.repeat(np.arange(nd), np.diff(cp_rp))
-    cp_pos = rp[rc] + ku[rc] + (np.arange(cp_rp[-1]) - cp_rp[rc])
+    class FakeSet:  # 3 u rows (nu = 1) + 1 p row, the layout fe_mixed_layout reports
+        ndofs = 4
+
+        class mesh:
+            nu = 1
+
+        @staticmethod
+        def csr_pattern():
+            return np.array([0, 5, 9, 13, 15]), None
+
+        @staticmethod
+        def mixed_layout():
+            return np.array([0, 4, 7, 10]), np.array([0, 1, 2, 3, 5])
+
+    uu_pos, cp_pos = N.mixed_positions(FakeSet())
     assert sorted(np.concatenate([uu_pos, cp_pos]).tolist()) == list(range(15))
+    # each displacement row: its uu entries first, then its coupling entries
+    assert uu_pos.tolist() == [0, 1, 2, 3, 5, 6, 7, 9, 10, 11]
+    assert cp_pos.tolist() == [4, 8, 12, 13, 14]
 
 
 # ------------------------------------------------------------------- GPU
