@@ -76,6 +76,25 @@ def test_stress_uniaxial_closed_form(oracle):
         assert abs(S[0] + S[1] + S[2]) < 1e-12 * (1 + abs(S[0]))  # p = 0: deviatoric
 
 
+def test_guccione_stress_uniaxial_closed_form(oracle):
+    """Guccione law (finite_elasticity_routines.f90:4419-4424) under isochoric
+    uniaxial stretch along the fibre: E = (C - I)/2 is diagonal,
+    Q = bf E11^2 + bt (E22^2 + E33^2), S_ii = C e^Q B_i E_i with
+    B = (bf, bt, bt), sigma_bar = F S F^T, and the deviator keeps
+    sigma_xx - sigma_yy = lam^2 S_11 - S_22 / lam."""
+    c = [0.88, 18.5, 3.58, 1.63]
+    for lam in (1.0, 1.03, 1.1, 0.95):
+        F = np.diag([lam, lam ** -0.5, lam ** -0.5])
+        S, _ = oracle.point_stress(M.GUCCIONE, c, F, 0.0)
+        e11, e22 = 0.5 * (lam ** 2 - 1.0), 0.5 * (1.0 / lam - 1.0)
+        q = c[1] * e11 ** 2 + 2.0 * c[2] * e22 ** 2
+        s11, s22 = c[0] * np.exp(q) * c[1] * e11, c[0] * np.exp(q) * c[2] * e22
+        expect = lam ** 2 * s11 - s22 / lam
+        assert abs((S[0] - S[1]) - expect) < 1e-12 * (1 + abs(expect))
+        assert abs(S[1] - S[2]) < 1e-13 and np.all(np.abs(S[3:]) < 1e-13)
+        assert abs(S[0] + S[1] + S[2]) < 1e-12 * (1 + abs(S[0]))
+
+
 @pytest.mark.parametrize("nxi,pmode", [(2, "element"), (3, "node")])
 def test_patch_uniaxial_residual(oracle, nxi, pmode):
     """Homogeneous uniaxial stretch: interior and pressure rows vanish, the
