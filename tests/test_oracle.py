@@ -95,6 +95,26 @@ def test_guccione_stress_uniaxial_closed_form(oracle):
         assert abs(S[0] + S[1] + S[2]) < 1e-12 * (1 + abs(S[0]))
 
 
+@pytest.mark.parametrize("law", ["mr", "guccione"])
+def test_rigid_motion_leaves_no_residual(oracle, law):
+    """Objectivity: a rigid rotation and translation of the undeformed body
+    (p = 0) gives C = I, so no stress and a zero residual, for the MR law and
+    for the Guccione law with a fibre field (its stress vanishes at E = 0)."""
+    if law == "mr":
+        m = M.regular_box(2, 2, 2, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0), perturb=0.1, seed=5)
+    else:
+        m = M.guccione_slab(2, 2, 2, lengths=(2.0, 2.0, 1.0), seed=5)
+    rng = np.random.default_rng(7)
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    if np.linalg.det(q) < 0:
+        q[:, 0] *= -1.0
+    x = np.concatenate([(q @ m.X + rng.normal(size=(3, 1))).ravel(), np.zeros(m.n_pressure)])
+    P = oracle.Problem(m)
+    rp, col = P.pattern()
+    _, r = P.assemble(x, rp, col, jacobian=False)
+    assert np.abs(r).max() < 1e-12
+
+
 @pytest.mark.parametrize("nxi,pmode", [(2, "element"), (3, "node")])
 def test_patch_uniaxial_residual(oracle, nxi, pmode):
     """Homogeneous uniaxial stretch: interior and pressure rows vanish, the
