@@ -163,6 +163,33 @@ def test_mixed_precision(torch, oracle, name, mode):
     assert abs(A - A.T).max() == 0.0
 
 
+@pytest.mark.parametrize("name", ["quad_node_mr_perturbed", "quad_node_guccione_fibres", "cfg1_lin_elem_mr"])
+def test_rigid_motion_leaves_no_residual(torch, name):
+    """Known answer on the CUDA path: a rigid rotation and translation of the
+    undeformed body with p = 0 has C = I, hence no stress and a zero
+    residual, for the FP64 and the mixed path alike."""
+    m = meshes()[name]
+    rng = np.random.default_rng(11)
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    if np.linalg.det(q) < 0:
+        q[:, 0] *= -1.0
+    x = np.concatenate([(q @ m.X + rng.normal(size=(3, 1))).ravel(), np.zeros(m.n_pressure)])
+    es = FiniteElasticityEquationsSet(m)
+    xd = torch.from_numpy(x).cuda()
+    r = es.residual_evaluate(xd)
+    es.check_status(xd)
+    assert float(r.abs().max()) < 1e-11
+    rm = torch.empty_like(xd)
+    es.jacobian_evaluate_mixed(xd, r=rm)
+    es.check_status(xd)
+    assert float(rm.abs().max()) < 1e-11
+    v = es.jacobian_evaluate(xd)
+    rf = torch.empty_like(xd)
+    es.jacobian_evaluate(xd, v, rf)
+    es.check_status(xd)
+    assert float(rf.abs().max()) < 1e-11
+
+
 def test_inverted_element_reports_numerical_error(torch):
     """A host-made fault: an element turned inside out gives FE_ERR_NUMERICAL
     (the kernel flags it, it does not trap)."""
