@@ -76,6 +76,24 @@ def test_stress_uniaxial_closed_form(oracle):
         assert abs(S[0] + S[1] + S[2]) < 1e-12 * (1 + abs(S[0]))  # p = 0: deviatoric
 
 
+def test_stress_simple_shear_closed_form(oracle):
+    """Mooney-Rivlin under simple shear F = I + gamma e1 (x) e2 (J = 1): the
+    classical results sigma_12 = 2 (c1 + c2) gamma,
+    sigma_11 - sigma_22 = 2 (c1 + c2) gamma^2 and
+    sigma_22 - sigma_33 = -2 c2 gamma^2, whatever the pressure."""
+    c1, c2 = 2.0, 6.0
+    for gamma in (0.0, 0.05, 0.3, -0.2):
+        F = np.eye(3)
+        F[0, 1] = gamma
+        S, _ = oracle.point_stress(M.MR, [c1, c2], F, 0.7)
+        tol = 1e-12 * (1.0 + abs(c1 + c2))
+        assert abs(S[3] - 2.0 * (c1 + c2) * gamma) < tol
+        assert abs((S[0] - S[1]) - 2.0 * (c1 + c2) * gamma ** 2) < tol
+        assert abs((S[1] - S[2]) + 2.0 * c2 * gamma ** 2) < tol
+        assert abs(S[4]) < tol and abs(S[5]) < tol
+        assert abs((S[0] + S[1] + S[2]) / 3.0 - 0.7) < tol  # the deviator carries no pressure
+
+
 def test_guccione_stress_uniaxial_closed_form(oracle):
     """Guccione law (finite_elasticity_routines.f90:4419-4424) under isochoric
     uniaxial stretch along the fibre: E = (C - I)/2 is diagonal,
