@@ -113,6 +113,34 @@ def test_guccione_stress_uniaxial_closed_form(oracle):
         assert abs(S[0] + S[1] + S[2]) < 1e-12 * (1 + abs(S[0]))
 
 
+@pytest.mark.parametrize("nxi,pmode", [(2, "element"), (3, "node")])
+def test_hydrostatic_pressure_traction(oracle, nxi, pmode):
+    """Undeformed box (z = X) with a uniform pressure p0: sigma = p0 I, so by
+    the divergence theorem the interior displacement rows vanish and each
+    face's rows add up to p0 times the face area along its outward normal;
+    the incompressibility rows vanish (J = 1)."""
+    p0 = -1.7
+    L = (1.5, 1.0, 0.5)
+    m = M.regular_box(2, 3, 2, lengths=L, nxi_u=nxi, pressure=pmode, law=M.MR, materials=(2.0, 6.0))
+    x = np.concatenate([m.X.ravel(), np.full(m.n_pressure, p0)])
+    P = oracle.Problem(m)
+    rp, col = P.pattern()
+    _, r = P.assemble(x, rp, col, jacobian=False)
+    nu = m.nu
+    i, j, k = m.node_ijk()
+    n1, n2, n3 = m.grid_u
+    idx = (i, j, k)
+    top = (n1 - 1, n2 - 1, n3 - 1)
+    area = (L[1] * L[2], L[0] * L[2], L[0] * L[1])
+    inner = (i > 0) & (i < n1 - 1) & (j > 0) & (j < n2 - 1) & (k > 0) & (k < n3 - 1)
+    for c in range(3):
+        rc = r[c * nu:(c + 1) * nu]
+        assert np.abs(rc[inner]).max(initial=0.0) < 1e-13
+        assert abs(rc[idx[c] == top[c]].sum() - p0 * area[c]) < 1e-12
+        assert abs(rc[idx[c] == 0].sum() + p0 * area[c]) < 1e-12
+    assert np.abs(r[3 * nu:]).max() < 1e-13
+
+
 @pytest.mark.parametrize("law", ["mr", "guccione"])
 def test_rigid_motion_leaves_no_residual(oracle, law):
     """Objectivity: a rigid rotation and translation of the undeformed body
