@@ -141,6 +141,69 @@ def test_hydrostatic_pressure_traction(oracle, nxi, pmode):
     assert np.abs(r[3 * nu:]).max() < 1e-13
 
 
+def _strain_energy(law, c, Cb):
+    """Strain energy of the isochoric right Cauchy-Green tensor: Mooney-Rivlin
+    c1 (I1 - 3) + c2 (I2 - 3), or Guccione (C/2)(e^Q - 1) with E = (Cb - I)/2 and
+    Q = bf E11^2 + bt (E22^2 + E33^2 + 2 E23^2) + 2 bfs (E12^2 + E13^2)."""
+    if law == M.MR:
+        I1 = np.trace(Cb)
+        I2 = 0.5 * (I1 ** 2 - np.trace(Cb @ Cb))
+        return c[0] * (I1 - 3.0) + c[1] * (I2 - 3.0)
+    E = 0.5 * (Cb - np.eye(3))
+    Q = (c[1] * E[0, 0] ** 2 + c[2] * (E[1, 1] ** 2 + E[2, 2] ** 2 + 2.0 * E[1, 2] ** 2)
+         + 2.0 * c[3] * (E[0, 1] ** 2 + E[0, 2] ** 2))
+    return 0.5 * c[0] * (np.exp(Q) - 1.0)
+
+
+def _energy(oracle, m, x, law, c):
+    """The discrete potential the residual is the gradient of:
+    Pi = sum_e sum_g w_g J_x [W(C_bar) + p (J - 1)], restated directly from
+    the strain energy (numpy, independent of the stress and residual code;
+    no fibre field, so the material frame is the global one)."""
+    gu, w, _ = oracle.basis_tables(m.nxi_u)
+    gp, _, _ = oracle.basis_tables(2)
+    nu = m.nu
+    z = x[:3 * nu].reshape(3, nu)
+    pr = x[3 * nu:]
+    total = 0.0
+    for e in range(m.ne):
+        nodes = m.elem_u[e]
+        Xe, ze = m.X[:, nodes], z[:, nodes]
+        for g in range(27):
+            dN = gu[g, 1:4, :]              # [xi_k][a]
+            dX, dz = Xe @ dN.T, ze @ dN.T   # [i][k]
+            F = dz @ np.linalg.inv(dX)
+            J = np.linalg.det(F)
+            Cb = J ** (-2.0 / 3.0) * (F.T @ F)
+            pg = pr[m.elem_p[e]] @ gp[g, 0, :] if m.elem_p is not None else pr[e]
+            total += w[g] * np.linalg.det(dX) * (_strain_energy(law, c, Cb) + pg * (J - 1.0))
+    return total
+
+
+@pytest.mark.parametrize("law", ["mr", "guccione"])
+@pytest.mark.parametrize("nxi,pmode", [(2, "element"), (3, "node")])
+def test_residual_is_the_gradient_of_the_energy(oracle, nxi, pmode, law):
+    """Variational consistency: the assembled residual equals the
+    central-difference gradient of the discrete potential (strain energy of
+    the isochoric right Cauchy-Green tensor plus p (J - 1)) at a general
+    deformed state, for the MR and the Guccione law."""
+    lw, c = (M.MR, (2.0, 6.0)) if law == "mr" else (M.GUCCIONE, (0.88, 18.5, 3.58, 1.63))
+    m = M.regular_box(1, 1, 2, lengths=(1.0, 0.8, 1.2), nxi_u=nxi, pressure=pmode, law=lw,
+                      materials=c, perturb=0.1, seed=2)
+    x = M.deformed_state(m, stretch=1.08, shear=0.06, noise=0.02, pressure=-1.3, seed=5)
+    P = oracle.Problem(m)
+    rp, col = P.pattern()
+    _, r = P.assemble(x, rp, col, jacobian=False)
+    h = 1e-6
+    fd = np.zeros_like(x)
+    for i in range(x.size):
+        xp, xm = x.copy(), x.copy()
+        xp[i] += h
+        xm[i] -= h
+        fd[i] = (_energy(oracle, m, xp, lw, c) - _energy(oracle, m, xm, lw, c)) / (2.0 * h)
+    assert np.abs(fd - r).max() < 1e-7 * np.abs(r).max()
+
+
 @pytest.mark.parametrize("law", ["mr", "guccione"])
 def test_rigid_motion_leaves_no_residual(oracle, law):
     """Objectivity: a rigid rotation and translation of the undeformed body
