@@ -155,11 +155,28 @@ def _strain_energy(law, c, Cb):
     return 0.5 * c[0] * (np.exp(Q) - 1.0)
 
 
+def _material_frame(dX, angles):
+    """dX/dnu of the material frame at a point (coordinate_routines.f90:
+    4042-4149): the orthonormal frame f = dX/dxi1, h = dX/dxi1 x dX/dxi2,
+    g = h x f, rotated by the fibre angle about its third axis, then the
+    imbrication angle about its second, then the sheet angle about its first."""
+    f = dX[:, 0]
+    h = np.cross(dX[:, 0], dX[:, 1])
+    g = np.cross(h, f)
+    R = np.stack([f / np.linalg.norm(f), g / np.linalg.norm(g), h / np.linalg.norm(h)], axis=1)
+    a, b, c = angles
+    Rz = np.array([[np.cos(a), -np.sin(a), 0.0], [np.sin(a), np.cos(a), 0.0], [0.0, 0.0, 1.0]])
+    Ry = np.array([[np.cos(b), 0.0, np.sin(b)], [0.0, 1.0, 0.0], [-np.sin(b), 0.0, np.cos(b)]])
+    Rx = np.array([[1.0, 0.0, 0.0], [0.0, np.cos(c), -np.sin(c)], [0.0, np.sin(c), np.cos(c)]])
+    return R @ Rz @ Ry @ Rx
+
+
 def _energy(oracle, m, x, law, c):
     """The discrete potential the residual is the gradient of:
     Pi = sum_e sum_g w_g J_x [W(C_bar) + p (J - 1)], restated directly from
-    the strain energy (numpy, independent of the stress and residual code;
-    no fibre field, so the material frame is the global one)."""
+    the strain energy (numpy, independent of the stress and residual code),
+    with C_bar in the material frame of the fibre field when the mesh has one
+    (angles interpolated from the nodes with the displacement basis)."""
     gu, w, _ = oracle.basis_tables(m.nxi_u)
     gp, _, _ = oracle.basis_tables(2)
     nu = m.nu
@@ -174,10 +191,35 @@ def _energy(oracle, m, x, law, c):
             dX, dz = Xe @ dN.T, ze @ dN.T   # [i][k]
             F = dz @ np.linalg.inv(dX)
             J = np.linalg.det(F)
+            if getattr(m, "fibre", None) is not None:
+                Q = _material_frame(dX, m.fibre[:, nodes] @ gu[g, 0, :])
+                F = F @ Q
             Cb = J ** (-2.0 / 3.0) * (F.T @ F)
             pg = pr[m.elem_p[e]] @ gp[g, 0, :] if m.elem_p is not None else pr[e]
             total += w[g] * np.linalg.det(dX) * (_strain_energy(law, c, Cb) + pg * (J - 1.0))
     return total
+
+
+def test_guccione_fibre_residual_is_the_gradient_of_the_energy(oracle):
+    """Variational consistency with a fibre field: the Guccione energy of
+    C_bar in the material frame (fibre angles varying through the
+    thickness, plus constant imbrication and sheet angles) has the assembled
+    residual as its gradient."""
+    c = (0.88, 18.5, 3.58, 1.63)
+    m = M.guccione_slab(1, 1, 2, lengths=(1.0, 0.8, 1.2), seed=2)
+    m.fibre = m.fibre + np.array([[0.0], [0.2], [-0.15]])
+    x = M.deformed_state(m, stretch=1.06, shear=0.05, noise=0.02, pressure=-0.4, seed=5)
+    P = oracle.Problem(m)
+    rp, col = P.pattern()
+    _, r = P.assemble(x, rp, col, jacobian=False)
+    h = 1e-6
+    fd = np.zeros_like(x)
+    for i in range(x.size):
+        xp, xm = x.copy(), x.copy()
+        xp[i] += h
+        xm[i] -= h
+        fd[i] = (_energy(oracle, m, xp, M.GUCCIONE, c) - _energy(oracle, m, xm, M.GUCCIONE, c)) / (2.0 * h)
+    assert np.abs(fd - r).max() < 1e-7 * np.abs(r).max()
 
 
 @pytest.mark.parametrize("law", ["mr", "guccione"])
