@@ -59,6 +59,7 @@ class FENewtonReport(C.Structure):
     _fields_ = [
         ("iterations", C.c_int32), ("converged", C.c_int32), ("linear_iterations", C.c_int64),
         ("residual_norm_initial", C.c_double), ("residual_norm", C.c_double), ("last_lambda", C.c_double),
+        ("line_search_failed", C.c_int32),
     ]
 
 
@@ -92,6 +93,7 @@ SIGNATURES = {
     "fe_batch_jacobian_evaluate_mixed": [_vp, _vp, _vp, _vp, _vp, _vp],
     "fe_batch_check": [_vp, _vp],
     "fe_batch_set_config": [_vp, _i32, _i32, _i32],
+    "fe_batch_set_barrier_limits": [_vp, C.c_uint32, C.c_uint32],
     "fe_batch_get_config": [_vp, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32), C.POINTER(C.c_double)],
     "fe_batch_autotune": [_vp, _vp, _vp, _vp, _vp, _i32, _vp],
     "fe_batch_capture": [_vp, _vp, _vp, _vp, _vp, _vp],

@@ -10,6 +10,8 @@
 
 #include <cooperative_groups.h>
 
+#include <atomic>
+
 namespace {
 
 constexpr int BT_THREADS = 256;
@@ -28,7 +30,8 @@ __device__ void grid_barrier(const BatchArgs& A) {
     const unsigned g = *gen;
     __threadfence();
     const unsigned arrived = atomicAdd(A.bar_count, 1u);
-    if (arrived == gridDim.x - 1) {
+    const unsigned limit = A.barrier_polls ? A.barrier_polls : BARRIER_POLLS;
+    if (arrived == gridDim.x - 1 + A.barrier_extra) {
       atomicExch(A.bar_count, 0u);
       __threadfence();
       atomicAdd(A.bar_gen, 1u);
@@ -38,7 +41,7 @@ __device__ void grid_barrier(const BatchArgs& A) {
       // CTAs still working on the colour
       unsigned polls = 0, ns = 64;
       while (*gen == g) {
-        if (++polls > BARRIER_POLLS) {
+        if (++polls > limit) {
           atomicOr(A.status, 2u);
           break;
         }
@@ -182,11 +185,15 @@ int launch_kernel(const BatchMember* members, int n, const BatchArgs& a, unsigne
                   int num_sms, cudaStream_t st) {
   using B = BatchCfg<EGQ, EGL>;
   auto kern = fe_mixed_batch_kernel<EGQ, EGL, MINB, TM, double>;
-  static bool attr = false;
-  if (!attr) {
+  // the attribute belongs to the device that is current: set once per device
+  static std::atomic<bool> attr[64];
+  int dev = 0;
+  cudaError_t e0 = cudaGetDevice(&dev);
+  if (e0 != cudaSuccess) return (int)e0;
+  if (dev < 0 || dev >= 64 || !attr[dev].load()) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, B::SMEM);
     if (e != cudaSuccess) return (int)e;
-    attr = true;
+    if (dev >= 0 && dev < 64) attr[dev].store(true);
   }
   const int smem = B::smem_for(mask);
   int per_sm = 0;

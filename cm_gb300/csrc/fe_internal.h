@@ -130,6 +130,9 @@ struct BatchArgs {
   unsigned* bar_count;       // grid barrier state (zero before a launch)
   unsigned* bar_gen;
   unsigned* status;          // bit 1: a grid barrier gave up waiting
+  unsigned barrier_polls;    // polls before a barrier gives up (0: the default limit)
+  unsigned barrier_extra;    // arrivals a barrier waits for beyond the grid (0; a diagnostic sets
+                             // 1 to make every barrier give up and report)
 };
 
 // Number of launch variants, their elements per group (triquadratic,

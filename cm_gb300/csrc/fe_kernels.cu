@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -502,6 +503,7 @@ struct fe_batch_s {
   std::vector<const void*> surf_sig;  // per member: d_surfp when loaded, else NULL
   unsigned* d_sync = nullptr;         // [0] barrier count, [1] barrier generation, [2] status
   int variant = 1, ctas_per_sm = 2, block_groups = 1;
+  unsigned barrier_polls = 0, barrier_extra = 0;  // grid-barrier limits (fe_batch_set_barrier_limits)
   unsigned type_mask = 0;             // element types present (bit 4: surface loads)
   double tuned_ms = -1.0;
   cudaGraph_t graph = nullptr;
@@ -516,7 +518,7 @@ namespace {
 template <int N1, int PM, int MODE>
 int launch_t(fe_handle h, KParams& kp, cudaStream_t st) {
   using C = Cfg<N1, PM>;
-  static bool attr_done[64] = {false};
+  static std::atomic<bool> attr_done[64];
   auto kern = fe_element_kernel<N1, PM, MODE>;
   const int dev = h->device;
   if (!attr_done[dev & 63]) {
@@ -784,6 +786,8 @@ int batch_launch_from(fe_batch b, const cmfe::BatchMember* table, cudaStream_t s
   a.bar_count = b->d_sync;
   a.bar_gen = b->d_sync + 1;
   a.status = b->d_sync + 2;
+  a.barrier_polls = b->barrier_polls;
+  a.barrier_extra = b->barrier_extra;
   const int e = cmfe::launch_mixed_batch(b->variant, b->type_mask, table, (int)b->members.size(), a, b->ctas_per_sm,
                                          b->num_sms, st);
   if (e != 0) return set_error(FE_ERR_CUDA, std::string("batched kernel launch: ") + cudaGetErrorString((cudaError_t)e));
@@ -904,6 +908,14 @@ int fe_create(const fe_mesh_desc* desc, fe_handle* out) {
   if (cudaMalloc(&h->d_status, sizeof(unsigned)) != cudaSuccess ||
       cudaMemset(h->d_status, 0, sizeof(unsigned)) != cudaSuccess)
     return fail(set_error(FE_ERR_CUDA, "status allocation failed"));
+  {
+    // Resolving the address of the allocation-free entry point's array loads
+    // the module that holds it, which commits its 16 MiB on this device now,
+    // at handle creation, rather than inside a later allocation-free call.
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    double* scratch = nullptr;
+    if ((rc = noalloc_scratch(h->device, &scratch))) return fail(rc);
+  }
   *out = h;
   return FE_NO_ERROR;
 }
@@ -1020,6 +1032,15 @@ int fe_residual_evaluate_noalloc(fe_handle h, const double* x, double* r, void* 
   double* dx = base;
   double* dr = base + FE_NOALLOC_MAX_DOFS;
   const size_t bytes = sizeof(double) * (size_t)h->hs.ndofs;
+  // Declared after the locks, so destroyed before them: every return below,
+  // the error returns included, first waits for the work this call queued on
+  // the shared array, and the next call cannot overwrite it in flight.
+  struct DrainOnReturn {
+    cudaStream_t st;
+    ~DrainOnReturn() {
+      if (cudaStreamSynchronize(st) != cudaSuccess) cudaGetLastError();
+    }
+  } drain{st};
   CUDA_TRY(cudaMemcpyAsync(dx, x, bytes, cudaMemcpyDefault, st));
   KParams kp = base_params(h);
   kp.x = dx;
@@ -1306,6 +1327,18 @@ int fe_batch_check(fe_batch b, void* stream) {
   if (v & 2u) return set_error(FE_ERR_CUDA, "batched launch: a grid barrier gave up waiting");
   for (fe_handle h : b->members)
     if ((rc = finish_status(h, st))) return rc;
+  return FE_NO_ERROR;
+}
+
+int fe_batch_set_barrier_limits(fe_batch b, uint32_t polls, uint32_t extra_arrivals) {
+  int rc = check_batch(b);
+  if (rc) return rc;
+  if (extra_arrivals > 1) return set_error(FE_ERR_INVALID_ARGUMENT, "extra_arrivals must be 0 or 1");
+  if (extra_arrivals && (polls == 0 || polls > 4096))
+    return set_error(FE_ERR_INVALID_ARGUMENT, "an unreachable barrier needs a poll limit in 1..4096");
+  std::lock_guard<std::mutex> lk(b->mu);
+  b->barrier_polls = polls;
+  b->barrier_extra = extra_arrivals;
   return FE_NO_ERROR;
 }
 

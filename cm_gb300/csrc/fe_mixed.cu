@@ -3,6 +3,8 @@
 // fe_mixed_impl.cuh.
 #include "fe_mixed_impl.cuh"
 
+#include <atomic>
+
 
 namespace {
 
@@ -19,12 +21,16 @@ __global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB) fe_mixed_kernel(KPa
 template <int N1, int PM, int SPLIT, class H>
 int launch_t(const KParams& kp, int num_sms, cudaStream_t st) {
   using C = MixCfg<N1, PM>;
-  static bool attr = false;
+  // the attribute belongs to the device that is current: set once per device
+  static std::atomic<bool> attr[64];
   auto kern = fe_mixed_kernel<N1, PM, SPLIT, H>;
-  if (!attr) {
+  int dev = 0;
+  cudaError_t e0 = cudaGetDevice(&dev);
+  if (e0 != cudaSuccess) return (int)e0;
+  if (dev < 0 || dev >= 64 || !attr[dev].load()) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
     if (e != cudaSuccess) return (int)e;
-    attr = true;
+    if (dev >= 0 && dev < 64) attr[dev].store(true);
   }
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::THREADS, C::SMEM);

@@ -469,6 +469,7 @@ int fe_newton_load_step(fe_handle h, const int32_t* fixed_dofs, const double* fi
     if (slope > 0.0) slope = -slope;
     const double f0 = 0.5 * fnorm * fnorm;
     double lam = 1.0, lam_prev = -1.0, f_prev = 0.0, f1 = 0.0;
+    bool accepted = false;
     NT_TRY(cudaMemcpyAsync(S.xs, xd, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     while (true) {
       NT_TRY(cudaMemcpyAsync(xd, S.xs, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
@@ -481,7 +482,10 @@ int fe_newton_load_step(fe_handle h, const int32_t* fixed_dofs, const double* fi
         if ((rc = S.dot_host(S.rn, S.rn, &q))) return finish(rc);
         f1 = 0.5 * q;
       }
-      if (std::isfinite(f1) && f1 <= f0 + o.alpha * lam * slope) break;
+      if (std::isfinite(f1) && f1 <= f0 + o.alpha * lam * slope) {
+        accepted = true;
+        break;
+      }
       if (lam < o.min_lambda) break;
       double lt;
       if (lam_prev < 0.0 || !std::isfinite(f1)) {
@@ -502,11 +506,18 @@ int fe_newton_load_step(fe_handle h, const int32_t* fixed_dofs, const double* fi
       lam = std::fmin(std::fmax(lt, 0.1 * lam), 0.5 * lam);
     }
     report->last_lambda = lam;
+    ++it;
+    if (!accepted) {
+      // No trial step gave sufficient decrease: keep the state, residual and
+      // norm from before the step (as PETSc's bt line search leaves X on a
+      // failed reduction) and stop.
+      NT_TRY(cudaMemcpyAsync(xd, S.xs, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      report->line_search_failed = 1;
+      break;
+    }
     std::swap(S.r, S.rn);
     fnorm_prev = fnorm;
-    fnorm = std::isfinite(f1) ? std::sqrt(2.0 * f1) : INFINITY;
-    ++it;
-    if (lam < o.min_lambda) break;
+    fnorm = std::sqrt(2.0 * f1);
   }
   report->iterations = it;
   report->residual_norm = fnorm;

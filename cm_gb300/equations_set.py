@@ -323,6 +323,12 @@ class EquationsSetBatch:
     def set_config(self, variant, ctas_per_sm, block_groups):
         check(_lib.load().fe_batch_set_config(self._b, variant, ctas_per_sm, block_groups))
 
+    def set_barrier_limits(self, polls=0, extra_arrivals=0):
+        """fe_batch_set_barrier_limits: diagnostic of the grid barrier's
+        failure path (extra_arrivals=1 makes every barrier give up after
+        `polls` polls; (0, 0) restores the default)."""
+        check(_lib.load().fe_batch_set_barrier_limits(self._b, polls, extra_arrivals))
+
     def config(self):
         v, c, g, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_double()
         check(_lib.load().fe_batch_get_config(self._b, C.byref(v), C.byref(c), C.byref(g), C.byref(ms)))

@@ -55,6 +55,7 @@ class StepReport:
     residual_norms: list = field(default_factory=list)
     linear_iterations: list = field(default_factory=list)
     line_search_lambdas: list = field(default_factory=list)
+    line_search_failed: bool = False
     seconds: float = 0.0
     assembly_seconds: float = 0.0
     linear_seconds: float = 0.0
@@ -396,6 +397,7 @@ class LoadStepSolver:
             if slope > 0:
                 slope = -slope
             lam, lam_prev, f_prev = 1.0, None, None
+            accepted = False
             x0 = x[free].clone()
             while True:
                 x[free] = x0 + lam * d
@@ -406,6 +408,7 @@ class LoadStepSolver:
                     rn = rn.clone()
                 f1 = 0.5 * float(rn @ rn)
                 if np.isfinite(f1) and f1 <= f0 + o.alpha * lam * slope:
+                    accepted = True
                     break
                 if lam < o.min_lambda:
                     break
@@ -425,12 +428,17 @@ class LoadStepSolver:
                 lam_prev, f_prev = lam, f1
                 lam = float(min(max(lt, 0.1 * lam), 0.5 * lam))
             rep.line_search_lambdas.append(lam)
+            it += 1
+            if not accepted:
+                # no step with sufficient decrease: keep the state from before
+                # the step (PETSc's bt line search leaves X on a failed
+                # reduction) and stop unconverged
+                x[free] = x0
+                rep.line_search_failed = True
+                break
             r = rn
             fnorm = float(r.norm())
             rep.residual_norms.append(fnorm)
-            it += 1
-            if lam < o.min_lambda:
-                break
         rep.iterations = it
         rep.converged = fnorm <= o.atol
         self._sync()

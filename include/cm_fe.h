@@ -230,6 +230,16 @@ int fe_batch_autotune(fe_batch b, const double* const* x, float* const* values_u
 int fe_batch_capture(fe_batch b, const double* const* x, float* const* values_uu,
                      double* const* values_coupling, double* const* r, void* stream);
 int fe_batch_replay(fe_batch b, void* stream);
+/* Diagnostic for the failure detection of the persistent launch (no
+ * counterpart in the reference).  The grid barrier between colours polls at
+ * most `polls` times (0: the default limit, a few seconds) and then gives up,
+ * sets the batch status word and lets the kernel run on and return;
+ * fe_batch_check then reports "a grid barrier gave up waiting".  With
+ * extra_arrivals = 1 every barrier waits for one CTA more than the grid has,
+ * so every barrier gives up: this exercises that path without a GPU fault
+ * (polls must then be 1..4096, so the launch still ends within milliseconds;
+ * its results are not valid).  (0, 0) restores the default. */
+int fe_batch_set_barrier_limits(fe_batch b, uint32_t polls, uint32_t extra_arrivals);
 /* Kernels the batch has run (a replay counts the kernels of its graph). */
 int fe_batch_launch_count(fe_batch b, int64_t* count);
 
@@ -252,10 +262,14 @@ int fe_batch_launch_count(fe_batch b, int64_t* count);
  *  - nothing in the array needs to start at zero: x is copied in whole and
  *    every residual entry is first stored, then added to, by the kernels;
  *  - the array is shared by every handle of a device, so overlapping calls
- *    would race on it: the library serialises them with a process-wide lock;
- *  - the first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress) and caches it, so it must come before any stream
- *    capture that would include the call. */
+ *    would race on it: the library serialises them with a process-wide lock,
+ *    and every return from the call (error returns included) first waits for
+ *    the work it queued on `stream`;
+ *  - fe_create looks up the array's device address (cudaGetSymbolAddress)
+ *    for its device and caches it; that lookup loads the library module that
+ *    holds the array, so the 16 MiB are committed on the device when the
+ *    first handle is created there, not inside a later call of this
+ *    function. */
 #define FE_NOALLOC_MAX_DOFS 1048576
 int fe_residual_evaluate_noalloc(fe_handle h, const double* x, double* r, void* stream);
 
@@ -277,7 +291,10 @@ int fe_residual_evaluate_noalloc(fe_handle h, const double* x, double* r, void* 
  * pressure rows), then takes a cubic backtracking line search on
  * 1/2 ||r_free||^2 (sufficient decrease alpha, step cap max_step); a trial
  * state with det F <= 0 counts as a failed trial step.  Everything runs on
- * the device; x may be host or device memory.  Returns FE_ERR_NUMERICAL when
+ * the device; x may be host or device memory.  When a line search finds no
+ * trial step with sufficient decrease (down to min_lambda), the step is
+ * rejected: x keeps the state from before it, the report says
+ * line_search_failed, and Newton stops unconverged.  Returns FE_ERR_NUMERICAL when
  * the initial state already has an inverted element, FE_NO_ERROR otherwise
  * (convergence is in the report). */
 typedef struct fe_newton_options {
@@ -299,6 +316,8 @@ typedef struct fe_newton_report {
   double residual_norm_initial;
   double residual_norm;       /* final ||r_free||_2 */
   double last_lambda;         /* step length of the last line search */
+  int32_t line_search_failed; /* 1 when the last line search found no step with sufficient
+                                 decrease; x is then the state from before that step */
 } fe_newton_report;
 
 void fe_newton_options_default(fe_newton_options* options);

@@ -213,3 +213,27 @@ def test_per_member_variant_is_the_single_set_path(torch):
     batch.check(xs[0])
     for (a, b, c), u, v, w in zip(refs, vus, vcs, rs):
         assert torch.equal(a, u) and torch.equal(b, v) and torch.equal(c, w)
+
+
+def test_grid_barrier_gives_up_and_reports(torch):
+    """The bounded grid-barrier wait of the persistent launch: with one
+    arrival more than the grid can give, every barrier gives up after 16
+    polls, the kernel still returns, and fe_batch_check reports the failure
+    instead of the launch hanging; after restoring the default limits the
+    same batch gives its normal, checked result again."""
+    from cm_gb300 import FEError
+    sets, xs, refs, b = _setup(torch)
+    b.set_config(0, 1, 1)  # a persistent variant (not the per-member launches)
+    vus, vcs, rs = b.allocate(xs[0].device)
+    b.set_barrier_limits(16, 1)
+    b.jacobian_evaluate_mixed(xs, vus, vcs, rs)
+    with pytest.raises(FEError, match="grid barrier gave up"):
+        b.check(xs[0])
+    b.set_barrier_limits(0, 0)
+    for t in vus + vcs + rs:
+        t.fill_(float("nan"))
+    b.jacobian_evaluate_mixed(xs, vus, vcs, rs)
+    b.check(xs[0])
+    _close(torch, refs, vus, vcs, rs)
+    with pytest.raises(FEError):
+        b.set_barrier_limits(0, 1)  # an unreachable barrier needs a small poll limit
