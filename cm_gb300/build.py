@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcm_fe.so")
-SOURCES = ["fe_batch.cu", "fe_batch_typed.cu", "fe_kernels.cu", "fe_mixed.cu", "fe_surface.cu", "fe_mlp.cu", "fe_pattern.cu", "fe_newton.cu", "fe_setup.cpp"]
+SOURCES = ["fe_batch.cu", "fe_batch_typed.cu", "fe_kernels.cu", "fe_mixed.cu", "fe_surface.cu", "fe_mlp.cu", "fe_pattern.cu", "fe_newton.cu", "fe_gather.cu", "fe_setup.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

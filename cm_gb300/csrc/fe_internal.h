@@ -57,6 +57,13 @@ struct HostSetup {
   // their boundary local faces (reference local-face order)
   std::vector<int32_t> bnd_elems, bnd_ptr;
   std::vector<uint8_t> bnd_mask;
+  // Row-node incidence for the staged assembly: the elements around every u
+  // node (sorted by element number, packed e * 32 + local node) and around
+  // every pressure row node (e * 8 + local pressure node).
+  std::vector<int32_t> u_inc_ptr, u_inc, p_inc_ptr, p_inc;
+  // shared memory one gather warp needs: the larger of a u node's three rows
+  // (3 x 3 wu FP32, then 3 x its pressure columns FP64) and a pressure row (FP64)
+  int gather_bytes = 0;
 };
 
 // Arguments of the element kernels (plain data; device pointers).
@@ -92,16 +99,39 @@ struct KParams {
   unsigned* status;
 };
 
+// Per-element records of the staged assembly (mixed kernel with staged
+// output, surface mode 2, row gather): the full displacement block
+// [e][3 NPE][3 NPE] (FP32, row-major), the pressure-coupling rows
+// [e][NPP][3 NPE] and the residual [e][nrow] (FP64).
+struct StageOut {
+  float* uu;
+  double* cp;
+  double* r;
+};
+
 // Launches the mixed-precision assembly kernel for one colour (fe_mixed.cu),
 // with the high-precision phases in FP64 or in double-float arithmetic.
 // Returns a cudaError_t value.
 int launch_mixed(const HostSetup& s, const KParams& kp, int num_sms, void* stream, bool double_float);
 
+// Launches the mixed-precision assembly kernel over all elements with its
+// output staged per element (so; fe_mixed.cu), in
+// one launch, without colour order.  Returns a cudaError_t value.
+int launch_mixed_staged(const HostSetup& s, const KParams& kp, const StageOut& so, int num_sms, void* stream,
+                        bool double_float);
+
+// Sums the staged element outputs into the CSR rows (uu FP32, coupling FP64)
+// and the residual, one row node at a time, in the fixed element order of
+// the incidence lists (fe_gather.cu).  Returns a cudaError_t value.
+int launch_gather(const HostSetup& s, const KParams& kp, const StageOut& so, const int32_t* u_inc_ptr,
+                  const int32_t* u_inc, const int32_t* p_inc_ptr, const int32_t* p_inc, int num_sms, void* stream);
+
 // Launches the surface-pressure kernel over boundary elements (fe_surface.cu):
-// mode 0 adds into the CSR values / residual, mode 1 into element outputs.
+// mode 0 adds into the CSR values / residual, mode 1 into element outputs,
+// mode 2 into the staged element records (so.uu, so.r).
 // Returns a cudaError_t value.
 int launch_surface(const HostSetup& s, const KParams& kp, const int32_t* belems, const uint8_t* bmask, int nb,
-                   int mode, int want_jac, int num_sms, void* stream);
+                   int mode, int want_jac, int num_sms, void* stream, const StageOut& so = StageOut{});
 
 // Builds the set-up; returns FE_NO_ERROR or a FE_ERR_* code with msg filled.
 int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg);

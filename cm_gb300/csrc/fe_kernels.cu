@@ -479,6 +479,12 @@ struct fe_equations_set {
   uint8_t* d_bnd_mask = nullptr;
   bool has_surfp = false;
   int high_precision = FE_HIGH_PRECISION_FP64;
+  int assembly_order = FE_ASSEMBLY_STAGED;
+  // staged assembly: incidence lists (uploaded at creation) and the
+  // per-element records (allocated on the first staged evaluation)
+  int32_t *d_u_inc_ptr = nullptr, *d_u_inc = nullptr, *d_p_inc_ptr = nullptr, *d_p_inc = nullptr;
+  float* d_st_uu = nullptr;
+  double *d_st_cp = nullptr, *d_st_r = nullptr;
   unsigned* d_status = nullptr;
   int32_t* d_col = nullptr;  // CSR columns on the device, uploaded on first use (Newton driver)
   // staging for calls given host memory
@@ -589,6 +595,47 @@ int surface_after(fe_handle h, const KParams& kp, int c, int want_jac, cudaStrea
   return FE_NO_ERROR;
 }
 
+// The staged mixed assembly into device buffers: one launch over all
+// elements into the per-element records, the surface-pressure faces added to
+// the records of their elements, then the row gather.  Adds the number of
+// kernels launched to *count when count is set.
+int ensure(void** buf, size_t bytes);
+
+int mixed_staged(fe_handle h, const double* dx, float* du, double* dc, double* dr, bool double_float,
+                 cudaStream_t st, int64_t* count) {
+  const auto& s = h->hs;
+  const size_t nu3 = 3 * (size_t)s.npe;
+  int rc;
+  if ((rc = ensure((void**)&h->d_st_uu, sizeof(float) * nu3 * nu3 * s.ne)) ||
+      (rc = ensure((void**)&h->d_st_cp, sizeof(double) * s.npp * nu3 * s.ne)) ||
+      (rc = ensure((void**)&h->d_st_r, sizeof(double) * s.nrow * (size_t)s.ne)))
+    return rc;
+  KParams kp = base_params(h);
+  kp.x = dx;
+  kp.vals_uu = du;
+  kp.vals = dc;
+  kp.r = dr;
+  const cmfe::StageOut so{h->d_st_uu, h->d_st_cp, h->d_st_r};
+  kp.elems = nullptr;
+  kp.first_elem = 0;
+  kp.count = s.ne;
+  int e = cmfe::launch_mixed_staged(s, kp, so, h->num_sms, st, double_float);
+  if (e != 0) return set_error(FE_ERR_CUDA, std::string("staged kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+  int64_t n = 1;
+  const int nb = s.bnd_ptr.empty() ? 0 : s.bnd_ptr[s.ncolours];
+  if (h->has_surfp && nb > 0) {
+    e = cmfe::launch_surface(s, kp, h->d_bnd_elems, h->d_bnd_mask, nb, 2, 1, h->num_sms, st, so);
+    if (e != 0) return set_error(FE_ERR_CUDA, std::string("surface kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+    ++n;
+  }
+  e = cmfe::launch_gather(s, kp, so, h->d_u_inc_ptr, h->d_u_inc, h->d_p_inc_ptr, h->d_p_inc, h->num_sms, st);
+  if (e != 0) return set_error(FE_ERR_CUDA, std::string("gather kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+  ++n;
+  h->launches += n;
+  if (count) *count += n;
+  return FE_NO_ERROR;
+}
+
 // Colour-by-colour launches over all elements.
 template <int MODE>
 int run_colours(fe_handle h, KParams kp, cudaStream_t st) {
@@ -606,6 +653,16 @@ int run_colours(fe_handle h, KParams kp, cudaStream_t st) {
 // The mixed assembly of one equations set into device buffers: one launch
 // per colour, each followed by that colour's surface-pressure faces.  Adds
 // the number of kernels launched to *count when count is set.
+int mixed_colours(fe_handle h, const double* dx, float* du, double* dc, double* dr, bool double_float,
+                  cudaStream_t st, int64_t* count);
+
+// The mixed assembly in the handle's assembly order.
+int mixed_assemble(fe_handle h, const double* dx, float* du, double* dc, double* dr, bool double_float,
+                   cudaStream_t st, int64_t* count) {
+  if (h->assembly_order == FE_ASSEMBLY_STAGED) return mixed_staged(h, dx, du, dc, dr, double_float, st, count);
+  return mixed_colours(h, dx, du, dc, dr, double_float, st, count);
+}
+
 int mixed_colours(fe_handle h, const double* dx, float* du, double* dc, double* dr, bool double_float,
                   cudaStream_t st, int64_t* count) {
   KParams kp = base_params(h);
@@ -771,7 +828,7 @@ int batch_launch_from(fe_batch b, const cmfe::BatchMember* table, cudaStream_t s
       const KParams& k = b->h_table[s].kp;
       fe_handle h = b->members[b->slot_member[s]];
       std::lock_guard<std::mutex> lk(h->mu);
-      const int rc = mixed_colours(h, k.x, k.vals_uu, k.vals, k.r, false, st, &b->launches);
+      const int rc = mixed_assemble(h, k.x, k.vals_uu, k.vals, k.r, false, st, &b->launches);
       if (rc) return rc;
     }
     return FE_NO_ERROR;
@@ -905,6 +962,9 @@ int fe_create(const fe_mesh_desc* desc, fe_handle* out) {
     if ((rc = dev_upload(&h->d_geo_dd, gdd))) return fail(rc);
   }
   if ((rc = dev_upload(&h->d_bnd_elems, s.bnd_elems)) || (rc = dev_upload(&h->d_bnd_mask, s.bnd_mask))) return fail(rc);
+  if ((rc = dev_upload(&h->d_u_inc_ptr, s.u_inc_ptr)) || (rc = dev_upload(&h->d_u_inc, s.u_inc)) ||
+      (rc = dev_upload(&h->d_p_inc_ptr, s.p_inc_ptr)) || (rc = dev_upload(&h->d_p_inc, s.p_inc)))
+    return fail(rc);
   if (cudaMalloc(&h->d_status, sizeof(unsigned)) != cudaSuccess ||
       cudaMemset(h->d_status, 0, sizeof(unsigned)) != cudaSuccess)
     return fail(set_error(FE_ERR_CUDA, "status allocation failed"));
@@ -925,7 +985,8 @@ int fe_destroy(fe_handle h) {
   void* ptrs[] = {h->d_surfp, h->d_bnd_elems, h->d_bnd_mask, h->d_geo_dd, h->d_elem_u, h->d_elem_p, h->d_row_ptr, h->d_uu_row_ptr, h->d_cp_row_ptr, h->d_wu,
                   h->d_wp, h->d_elem_table, h->d_colour_elems, h->d_tables, h->d_geo, h->d_mat,
                   h->d_gbf_u, h->d_gbf_p, h->d_gw, h->d_status, h->s_x, h->s_r, h->s_vals, h->s_cp,
-                  h->s_uu, h->s_elem, h->d_col};
+                  h->s_uu, h->s_elem, h->d_col, h->d_u_inc_ptr, h->d_u_inc, h->d_p_inc_ptr, h->d_p_inc,
+                  h->d_st_uu, h->d_st_cp, h->d_st_r};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete h;
@@ -1117,7 +1178,7 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
     if ((rc = ensure((void**)&h->s_r, sizeof(double) * h->hs.ndofs))) return rc;
     dr = h->s_r;
   }
-  if ((rc = mixed_colours(h, dx, du, dc, dr, h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT, st, nullptr)))
+  if ((rc = mixed_assemble(h, dx, du, dc, dr, h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT, st, nullptr)))
     return rc;
   if (hu) CUDA_TRY(cudaMemcpyAsync(values_uu, du, sizeof(float) * h->hs.nnz_uu, cudaMemcpyDeviceToHost, st));
   if (hc) CUDA_TRY(cudaMemcpyAsync(values_coupling, dc, sizeof(double) * h->hs.nnz_cp, cudaMemcpyDeviceToHost, st));
@@ -1209,6 +1270,15 @@ int fe_set_high_precision(fe_handle h, int32_t mode) {
   if (mode != FE_HIGH_PRECISION_FP64 && mode != FE_HIGH_PRECISION_DOUBLE_FLOAT)
     return set_error(FE_ERR_INVALID_ARGUMENT, "unknown high-precision mode");
   h->high_precision = mode;
+  return FE_NO_ERROR;
+}
+
+int fe_set_assembly_order(fe_handle h, int32_t order) {
+  if (!h) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL handle");
+  if (order != FE_ASSEMBLY_STAGED && order != FE_ASSEMBLY_COLOURED)
+    return set_error(FE_ERR_INVALID_ARGUMENT, "unknown assembly order");
+  std::lock_guard<std::mutex> lk(h->mu);
+  h->assembly_order = order;
   return FE_NO_ERROR;
 }
 

@@ -315,12 +315,20 @@ __device__ __forceinline__ void mix_tables(const KParams& P, unsigned char* sm) 
   }
 }
 
+// Element number of entry i of an element list (NULL: P.first_elem + i).
+__device__ __forceinline__ int elem_at(const KParams& P, const int32_t* elems, int i) {
+  return elems ? elems[i] : P.first_elem + i;
+}
+
 // One group of up to EG elements, elems[grp*EG ...] of the count elements
 // of the current colour.  p4_first swaps the order of the independent FP64
-// (P3) and tensor-core (P4) stages.
-template <int N1, int PM, int EG_, int SPLIT, class H>
+// (P3) and tensor-core (P4) stages.  OUT = 0 adds the element's entries into
+// the CSR values and the residual (first contributor in colour order stores,
+// later ones add); OUT = 1 stores them into the element's staging records
+// (*SO), which the row gather sums afterwards.
+template <int N1, int PM, int EG_, int SPLIT, class H, int OUT = 0>
 __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems, int count, int grp, bool p4_first,
-                                          unsigned char* sm) {
+                                          unsigned char* sm, const cmfe::StageOut* SO = nullptr) {
   using C = MixCfg<N1, PM, EG_>;
   constexpr int NPE = C::NPE, NPP = C::NPP, NR = C::NR, NU3 = C::NU3, NROW = C::NROW, EG = C::EG;
   constexpr int KPW = C::KPW;
@@ -349,7 +357,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
     const int el = i / (NR + 1), r = i % (NR + 1);
     int v = 0;
     if (el < nvalid) {
-      const int e = elems[grp * EG + el];
+      const int e = elem_at(P, elems, grp * EG + el);
       if (r < NPE)
         v = P.elem_u[(size_t)e * NPE + r];
       else if (r < NR)
@@ -434,7 +442,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
     for (int t = tid; t < EG * NG; t += HALF) {
       const int el = t / NG, g = t % NG;
       if (el >= nvalid) continue;
-      const int e = elems[grp * EG + el];
+      const int e = elem_at(P, elems, grp * EG + el);
       H M[3][3], adj[3][3];
 #pragma unroll
       for (int c = 0; c < 3; ++c)
@@ -491,7 +499,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
     for (int t = tid - HALF; t < (P.res_only ? 0 : EG * NG); t += HALF) {
       const int el = t / NG, g = t % NG;
       if (el >= nvalid) continue;
-      const int e = elems[grp * EG + el];
+      const int e = elem_at(P, elems, grp * EG + el);
       float Mf[3][3], Ff[3][3], cf[4], Cf[6][6], Sf[6], inv[3][3];
 #pragma unroll
       for (int c = 0; c < 3; ++c)
@@ -632,12 +640,16 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
             ln = NPE + q;
             R = (size_t)3 * nu + nd[ln];
           }
-          const bool first = tab[ln * NR + ln] & 0x8000;
           const double accd = hd(acc);
-          if (first)
-            P.r[R] = accd;
-          else
-            atomicAdd(&P.r[R], accd);
+          if constexpr (OUT == 1) {
+            SO->r[(size_t)elem_at(P, elems, grp * EG + el) * NROW + row] = accd;
+          } else {
+            const bool first = tab[ln * NR + ln] & 0x8000;
+            if (first)
+              P.r[R] = accd;
+            else
+              atomicAdd(&P.r[R], accd);
+          }
         }
       }
       if (!PM && !P.res_only) {
@@ -651,6 +663,10 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
           const uint16_t* tab = P.tables + (size_t)nd[NR] * NR * NR;
           const H* rk = &s_dz[(el * 9 + n * 3) * NPE + b];
           const double kv = hd(rk[0] + rk[NPE] + rk[2 * NPE]);
+          if constexpr (OUT == 1) {
+            SO->cp[(size_t)elem_at(P, elems, grp * EG + el) * NU3 + col] = kv;
+            continue;
+          }
           const int nb = nd[b], pq = nd[NPE];
           const uint16_t tqb = tab[NPE * NR + b], tbq = tab[b * NR + NPE];
           const size_t p1 = (size_t)P.cp_row_ptr[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (tqb & 0x7fff);
@@ -725,9 +741,13 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
               for (int g3 = 0; g3 < 3; ++g3)
                 acc = hfma(LD[(q3 * 3 + g3) * N1 + b3], u[g3], hfma(LB[(q3 * 3 + g3) * N1 + b3], w[g3], acc));
               const int q = q1 + 2 * q2 + 4 * q3, b = b1 + N1 * b2 + N2 * b3;
+              const double kv = hd(acc);
+              if constexpr (OUT == 1) {
+                SO->cp[((size_t)elem_at(P, elems, grp * EG + el) * 8 + q) * NU3 + n * NPE + b] = kv;
+                continue;
+              }
               const int lq = NPE + q, pq = nd[lq], nb = nd[b];
               const uint16_t tqb = tab[lq * NR + b], tbq = tab[b * NR + lq];
-              const double kv = hd(acc);
               const size_t p1 = (size_t)P.cp_row_ptr[(size_t)3 * nu + pq] + (size_t)n * P.wp[pq] + (tqb & 0x7fff);
               if (tqb & 0x8000)
                 P.vals[p1] = kv;
@@ -742,7 +762,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
         }
       }
       // structurally zero pressure-pressure entries, stored by their first contributor
-      for (int i = tid; i < (P.res_only ? 0 : EG * NPP * NPP); i += C::THREADS) {
+      for (int i = tid; i < (P.res_only || OUT == 1 ? 0 : EG * NPP * NPP); i += C::THREADS) {
         const int el = i / (NPP * NPP), q = (i / NPP) % NPP, q2 = i % NPP;
         if (el >= nvalid) continue;
         const int* nd = &s_node[el * (NR + 1)];
@@ -775,17 +795,19 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
         int* s_base = reinterpret_cast<int*>(s_dz);
         uint16_t* s_tab = reinterpret_cast<uint16_t*>(s_f32);
         __syncthreads();
-        for (int i = tid; i < EG * 9 * NPE; i += C::THREADS) {
-          const int a = i % NPE, mn = (i / NPE) % 9, el = i / (9 * NPE);
-          const int na = s_node[el * (NR + 1) + a];
-          s_base[i] = el < nvalid ? P.uu_row_ptr[(size_t)(mn / 3) * nu + na] + (mn % 3) * P.wu[na] : 0;
+        if constexpr (OUT == 0) {
+          for (int i = tid; i < EG * 9 * NPE; i += C::THREADS) {
+            const int a = i % NPE, mn = (i / NPE) % 9, el = i / (9 * NPE);
+            const int na = s_node[el * (NR + 1) + a];
+            s_base[i] = el < nvalid ? P.uu_row_ptr[(size_t)(mn / 3) * nu + na] + (mn % 3) * P.wu[na] : 0;
+          }
+          for (int i = tid; i < EG * NPE * NPE; i += C::THREADS) {
+            const int ab = i % (NPE * NPE), el = i / (NPE * NPE);
+            const int a = ab / NPE, b = ab % NPE;
+            s_tab[i] = el < nvalid ? P.tables[(size_t)s_node[el * (NR + 1) + NR] * NR * NR + a * NR + b] : 0;
+          }
+          __syncthreads();
         }
-        for (int i = tid; i < EG * NPE * NPE; i += C::THREADS) {
-          const int ab = i % (NPE * NPE), el = i / (NPE * NPE);
-          const int a = ab / NPE, b = ab % NPE;
-          s_tab[i] = el < nvalid ? P.tables[(size_t)s_node[el * (NR + 1) + NR] * NR * NR + a * NR + b] : 0;
-        }
-        __syncthreads();
         for (int task = warp; task < nvalid * MT2; task += C::THREADS / 32) {
           const int el = task / MT2, mt = task % MT2;
           const int* bs = &s_base[el * 9 * NPE];
@@ -868,6 +890,12 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
               blk_mn(blk, m, n);
               if (m == n && a < b) continue;
               const float v = acc[nt][h];
+              if constexpr (OUT == 1) {
+                float* st = SO->uu + (size_t)elem_at(P, elems, grp * EG + el) * NU3 * NU3;
+                st[(size_t)(m * NPE + a) * NU3 + n * NPE + b] = v;
+                if (!(m == n && a == b)) st[(size_t)(n * NPE + b) * NU3 + m * NPE + a] = v;
+                continue;
+              }
               const uint16_t tab_ab = tb[a * NPE + b];
               const int p1 = bs[(m * 3 + n) * NPE + a] + (tab_ab & 0x7fff);
               if (tab_ab & 0x8000)

@@ -232,6 +232,31 @@ int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg) {
   for (int n = 0; n < s.nu; ++n)
     if (surr_u[n].empty()) return fail(msg, "a u node belongs to no element");
 
+  // Incidence lists of the staged assembly (elements in increasing order).
+  s.u_inc_ptr.assign((size_t)s.nu + 1, 0);
+  s.p_inc_ptr.assign((size_t)s.npn + 1, 0);
+  for (int n = 0; n < s.nu; ++n) s.u_inc_ptr[n + 1] = s.u_inc_ptr[n] + (int32_t)surr_u[n].size();
+  for (int q = 0; q < s.npn; ++q) s.p_inc_ptr[q + 1] = s.p_inc_ptr[q] + (int32_t)surr_p[q].size();
+  s.u_inc.resize(s.u_inc_ptr[s.nu]);
+  s.p_inc.resize(s.p_inc_ptr[s.npn]);
+  if ((int64_t)s.ne * 32 >= (1ll << 31)) return fail(msg, "too many elements for the staged assembly's incidence lists");
+  parallel_for(s.nu, [&](int n) {
+    int32_t k = s.u_inc_ptr[n];
+    for (int e : surr_u[n]) {
+      int la = 0;
+      while (unode(e, la) != n) ++la;
+      s.u_inc[k++] = e * 32 + la;
+    }
+  });
+  parallel_for(s.npn, [&](int q) {
+    int32_t k = s.p_inc_ptr[q];
+    for (int e : surr_p[q]) {
+      int lq = 0;
+      while (pnode(e, lq) != q) ++lq;
+      s.p_inc[k++] = e * 8 + lq;
+    }
+  });
+
   // Neighbourhoods: sorted u nodes and sorted pressure row nodes around every row node.
   std::vector<std::vector<int32_t>> nbu_u(s.nu), nbp_u(s.nu), nbu_p(s.npn), nbp_p(s.npn);
   auto fill_nb = [&](const std::vector<int32_t>& elems, std::vector<int32_t>& nu_out, std::vector<int32_t>& np_out) {
@@ -275,6 +300,18 @@ int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg) {
   s.nnz = nnz;
   s.nnz_uu = nuu;
   s.nnz_cp = ncp;
+  {
+    int64_t need = 0;
+    for (int n = 0; n < s.nu; ++n) {
+      const int64_t wc = s.cp_row_ptr[(size_t)n + 1] - s.cp_row_ptr[(size_t)n];
+      need = std::max<int64_t>(need, ((36 * (int64_t)s.wu[n] + 15) & ~(int64_t)15) + 3 * wc * 8);
+    }
+    for (int q = 0; q < s.npn; ++q) {
+      const size_t row = (size_t)3 * s.nu + q;
+      need = std::max<int64_t>(need, (int64_t)(s.cp_row_ptr[row + 1] - s.cp_row_ptr[row]) * 8);
+    }
+    s.gather_bytes = (int)std::min<int64_t>((need + 15) & ~(int64_t)15, 1 << 30);
+  }
   s.col.allocate(nnz);
   parallel_for((int)s.ndofs, [&](int r) {
     const bool urow = r < 3ll * s.nu;

@@ -53,10 +53,12 @@ struct SurfWarpSmem {
 // All loaded faces of boundary element e, by one warp (S is the warp's
 // shared scratch).  mode: 0 = CSR (FP64 values, or FP32 uu values when
 // P.vals_uu), 1 = element outputs (P.elem_out, elements first_elem ..
-// first_elem + count - 1).
+// first_elem + count - 1), 2 = the element's staging records (SO->uu,
+// SO->r), which only this warp touches, so it adds without atomics.
 template <int N1>
 __device__ __forceinline__ void surface_element(const cmfe::KParams& P, int e, const uint8_t* bmask, int mode,
-                                                int want_jac, SurfWarpSmem& S, int lane) {
+                                                int want_jac, SurfWarpSmem& S, int lane,
+                                                const cmfe::StageOut* SO = nullptr) {
   constexpr int NPE = N1 * N1 * N1, NF = N1 * N1;
   const int nr = P.nr, nrow = 3 * NPE + (P.pmode ? 8 : 1);
   const uint8_t mask = bmask[e];
@@ -117,7 +119,7 @@ __device__ __forceinline__ void surface_element(const cmfe::KParams& P, int e, c
     const uint16_t* tab = P.tables + (size_t)P.elem_table[e] * nr * nr;
     const int* en = P.elem_u + (size_t)e * NPE;
     // residual rows
-    if (P.r != nullptr || (mode == 1 && !want_jac)) {
+    if (P.r != nullptr || (mode == 1 && !want_jac) || mode == 2) {
       if (lane < 3 * NF) {
         const int c = lane / NF, f = lane % NF;
         const double x3[3] = {(-sqrt(0.6) + 1.0) / 2.0, 0.5, (sqrt(0.6) + 1.0) / 2.0};
@@ -127,7 +129,9 @@ __device__ __forceinline__ void surface_element(const cmfe::KParams& P, int e, c
           acc = fma(S.gq[ng][0] * S.gq[ng][1 + c], N, acc);
         }
         const int a = S.node[f];
-        if (mode == 1) {
+        if (mode == 2) {
+          SO->r[(size_t)e * nrow + c * NPE + a] += acc;
+        } else if (mode == 1) {
           P.elem_out[(size_t)(e - P.first_elem) * nrow + c * NPE + a] += acc;
         } else {
           atomicAdd(&P.r[(size_t)c * P.nu + en[a]], acc);
@@ -153,6 +157,15 @@ __device__ __forceinline__ void surface_element(const cmfe::KParams& P, int e, c
         acc += (w0 * dn0) * nm + (w1 * dn1) * nm;
       }
       const int a = S.node[ms], b = S.node[ns];
+      if (mode == 2) {
+        // the lower block entry and its mirror: distinct entries for distinct
+        // (oh, ms, ns), so the lanes never touch the same word
+        float* st = SO->uu + (size_t)e * (3 * NPE) * (3 * NPE);
+        const int R = mh * NPE + a, Cc = nh * NPE + b;
+        st[(size_t)R * (3 * NPE) + Cc] += (float)acc;
+        st[(size_t)Cc * (3 * NPE) + R] += (float)acc;
+        continue;
+      }
       if (mode == 1) {
         double* out = P.elem_out + (size_t)(e - P.first_elem) * nrow * nrow;
         const int R = mh * NPE + a, Cc = nh * NPE + b;

@@ -222,6 +222,14 @@ class FiniteElasticityEquationsSet:
         check(_lib.load().fe_set_high_precision(self._h, code))
         self.high_precision = mode
 
+    def set_assembly_order(self, order):
+        """fe_set_assembly_order: "staged" (per-element records and a row
+        gather, the default) or "coloured" (element colours adding into the
+        CSR arrays) for jacobian_evaluate_mixed."""
+        code = {"staged": _lib.FE_ASSEMBLY_STAGED, "coloured": _lib.FE_ASSEMBLY_COLOURED}[order]
+        check(_lib.load().fe_set_assembly_order(self._h, code))
+        self.assembly_order = order
+
     def newton_load_step(self, x, fixed_dofs, fixed_values, **options):
         """fe_newton_load_step: one load increment by Newton on the device
         (FP64 Jacobian, block-diagonal-preconditioned GMRES, cubic

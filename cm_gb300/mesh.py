@@ -177,3 +177,40 @@ def guccione_slab(ex=64, ey=64, ez=16, lengths=(40.0, 40.0, 10.0), angle_range_d
     ang = ang + np.deg2rad(rng.uniform(-noise_deg, noise_deg, size=m.nu))
     m.fibre = np.stack([ang, np.zeros(m.nu), np.zeros(m.nu)])
     return m
+
+
+def thick_cylinder(n_r=2, n_theta=8, n_z=1, r_in=0.5, r_out=1.0, height=1.0, law=MR, materials=(2.0, 6.0)) -> Mesh:
+    """Thick-walled cylinder (tube) of triquadratic displacement / trilinear
+    nodal pressure elements, the geometry of the reference's cylinder
+    generated mesh (GENERATED_MESH_CYLINDER_MESH_TYPE) on which its analytic
+    inflation-extension solution is posed: xi1 radial (inner surface normal
+    -xi1, outer +xi1), xi2 circumferential, xi3 axial (bottom -xi3, top +xi3),
+    generated_mesh_routines.f90:4193-4280.  Nodes lie on exact circles; the
+    circumferential direction wraps around (the last element shares the
+    nodes at theta = 0).  Nodes are numbered radial fastest, then
+    circumferential, then axial (this generator's own numbering); grid_u
+    holds the node counts (radial, circumferential, axial)."""
+    n1 = 3
+    NR, NT, NZ = 2 * n_r + 1, 2 * n_theta, 2 * n_z + 1
+    nu = NR * NT * NZ
+    idx = np.arange(nu)
+    i, j, k = idx % NR, (idx // NR) % NT, idx // (NR * NT)
+    r = r_in + (r_out - r_in) * i / (NR - 1)
+    th = 2.0 * np.pi * j / NT
+    X = np.stack([r * np.cos(th), r * np.sin(th), height * k / (NZ - 1)])
+    er, et, ez = np.meshgrid(np.arange(n_r), np.arange(n_theta), np.arange(n_z), indexing="ij")
+    er, et, ez = (a.transpose(2, 1, 0).ravel() for a in (er, et, ez))  # radial fastest
+    a1, a2, a3 = np.meshgrid(np.arange(n1), np.arange(n1), np.arange(n1), indexing="ij")
+    a1, a2, a3 = (a.transpose(2, 1, 0).ravel() for a in (a1, a2, a3))
+    gi = 2 * er[:, None] + a1[None, :]
+    gj = (2 * et[:, None] + a2[None, :]) % NT
+    gk = 2 * ez[:, None] + a3[None, :]
+    elem_u = (gi + NR * gj + NR * NT * gk).astype(np.int32)
+    corners = [(a * (n1 - 1)) + (b * (n1 - 1)) * n1 + (c * (n1 - 1)) * n1 * n1
+               for c in (0, 1) for b in (0, 1) for a in (0, 1)]
+    users = elem_u[:, corners]
+    uniq = np.unique(users)
+    elem_p = np.searchsorted(uniq, users).astype(np.int32)
+    return Mesh(dims=(n_r, n_theta, n_z), lengths=(r_out - r_in, 2.0 * np.pi * r_in, height), nxi_u=n1,
+                p_mode=FE_PRESSURE_NODE_BASED, law=law, elem_u=elem_u, elem_p=elem_p, X=X,
+                materials=np.asarray(materials, dtype=np.float64), fibre=None, grid_u=(NR, NT, NZ))

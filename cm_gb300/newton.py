@@ -527,3 +527,39 @@ def bottom_face_pressure(mesh, value):
     sp = np.zeros((3, mesh.nu))
     sp[2, k == 0] = value
     return sp
+
+
+def cylinder_conditions(mesh, stretch):
+    """Dirichlet conditions of the reference's cylinder inflation-extension
+    problem (FiniteElasticity_BoundaryConditionsAnalyticCalculate,
+    finite_elasticity_routines.f90:132-484) on a `mesh.thick_cylinder` mesh:
+    z fixed to 0 on the bottom and to stretch * Z on the top (here raised with
+    the load increments, fixed-incremented), and on the bottom the x (y)
+    component fixed to 0 at the nodes with |X| < 1e-7 (|Y| < 1e-7), which
+    removes the rigid rotation and translation."""
+    _, _, k = mesh.node_ijk()
+    nz = mesh.grid_u[2]
+    X = mesh.X
+    nu = mesh.nu
+    bc = DirichletConditions(mesh.ndofs)
+    bottom = np.nonzero(k == 0)[0]
+    top = np.nonzero(k == nz - 1)[0]
+    bc.fix(2 * nu + bottom, 0.0)
+    bc.fix(2 * nu + top, stretch * X[2, top], incremented=True)
+    bx = bottom[np.abs(X[0, bottom]) < 1e-7]
+    by = bottom[np.abs(X[1, bottom]) < 1e-7]
+    bc.fix(bx, 0.0)
+    bc.fix(nu + by, 0.0)
+    return bc
+
+
+def cylinder_pressure(mesh, p_inner, p_outer):
+    """[3][nu] surface pressure of the cylinder problem: p_inner on the inner
+    surface and p_outer on the outer surface, both on faces normal to xi1
+    (the reference stores them on component |normal xi| = 1 of the DELUDELN
+    variable, finite_elasticity_routines.f90:196-223)."""
+    i, _, _ = mesh.node_ijk()
+    sp = np.zeros((3, mesh.nu))
+    sp[0, i == 0] = p_inner
+    sp[0, i == mesh.grid_u[0] - 1] = p_outer
+    return sp

@@ -172,6 +172,27 @@ int fe_set_materials(fe_handle h, const double* materials);
 #define FE_HIGH_PRECISION_DOUBLE_FLOAT 1
 int fe_set_high_precision(fe_handle h, int32_t mode);
 
+/* How fe_jacobian_evaluate_mixed adds the element contributions into the
+ * CSR values and the residual (both deterministic; no counterpart in the
+ * reference, which adds element by element, MATRIX_VALUES_ADD_DP2,
+ * matrix_vector.f90:2756-2880).
+ * FE_ASSEMBLY_STAGED (the default): one launch evaluates every element and
+ * stores its entries in per-element records on the device; a second kernel
+ * then forms each CSR row once from the records of the elements around the
+ * row's node, in increasing element number.  Every matrix sector is written
+ * once and never read.  The records take, per element, 4 (3 n_p)^2 +
+ * 8 n_q 3 n_p + 8 (3 n_p + n_q) bytes (32 kB for a triquadratic element with
+ * nodal pressure), allocated on the first staged evaluation and kept with
+ * the handle.
+ * FE_ASSEMBLY_COLOURED: one launch per element colour, each element adding
+ * its entries straight into the CSR arrays (the first contributor in colour
+ * order stores, later ones add).  No extra memory.
+ * The two orders sum in different orders, so they agree to rounding, not
+ * bit for bit; each is bit-reproducible. */
+#define FE_ASSEMBLY_STAGED 0
+#define FE_ASSEMBLY_COLOURED 1
+int fe_set_assembly_order(fe_handle h, int32_t order);
+
 /* Element-level evaluation for a contiguous range of elements (0-based), the
  * direct counterparts of FiniteElasticity_FiniteElementResidualEvaluate /
  * ..JacobianEvaluate(EQUATIONS_SET, ELEMENT_NUMBER).  Element matrices are

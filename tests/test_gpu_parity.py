@@ -113,10 +113,13 @@ def test_deterministic(torch):
     a = es.jacobian_evaluate(x).clone()
     b = es.jacobian_evaluate(x).clone()
     assert torch.equal(a, b)
-    ua, ca = es.jacobian_evaluate_mixed(x)
-    ua, ca = ua.clone(), ca.clone()
-    ub, cb = es.jacobian_evaluate_mixed(x)
-    assert torch.equal(ua, ub) and torch.equal(ca, cb)
+    for order in ("staged", "coloured"):
+        es.set_assembly_order(order)
+        ra, rb = torch.empty_like(x), torch.empty_like(x)
+        ua, ca = es.jacobian_evaluate_mixed(x, r=ra)
+        ua, ca = ua.clone(), ca.clone()
+        ub, cb = es.jacobian_evaluate_mixed(x, r=rb)
+        assert torch.equal(ua, ub) and torch.equal(ca, cb) and torch.equal(ra, rb), order
 
 
 MIXED_UU_TOL = 1e-4  # BF16x3 tensor-core products, FP32 accumulation, relative to the largest entry
@@ -125,13 +128,15 @@ MIXED_UU_TOL = 1e-4  # BF16x3 tensor-core products, FP32 accumulation, relative 
 REL_DD, FLOOR_DD = 1e-11, 1e-12
 
 
+@pytest.mark.parametrize("order", ["staged", "coloured"])
 @pytest.mark.parametrize("mode", ["fp64", "double_float"])
 @pytest.mark.parametrize("name", list(meshes()))
-def test_mixed_precision(torch, oracle, name, mode):
+def test_mixed_precision(torch, oracle, name, mode, order):
     """High-precision parts of the mixed path (coupling blocks, residual)
     match the oracle at the FP64 tolerance (fp64 mode) or the double-float
     tolerance; the FP32 displacement block matches it to MIXED_UU_TOL of the
-    largest entry."""
+    largest entry; for both assembly orders (per-element records and a row
+    gather, or colour-ordered adds into the CSR arrays)."""
     m = meshes()[name]
     x = state(m)
     P = oracle.Problem(m)
@@ -139,6 +144,7 @@ def test_mixed_precision(torch, oracle, name, mode):
     vo, ro = P.assemble(x, rp_o, col_o, nthreads=1)
     es = FiniteElasticityEquationsSet(m)
     es.set_high_precision(mode)
+    es.set_assembly_order(order)
     rel, floor = (REL, FLOOR) if mode == "fp64" else (REL_DD, FLOOR_DD)
     xd = torch.from_numpy(x).cuda()
     rm = torch.empty_like(xd)
@@ -152,8 +158,11 @@ def test_mixed_precision(torch, oracle, name, mode):
         is_uu[rp[r]:rp[r] + (uu_rp[r + 1] - uu_rp[r])] = True
     assert_entrywise(full[~is_uu], vo[~is_uu], rel, floor, what=name + " mixed coupling blocks")
     assert_entrywise(rm.cpu().numpy(), ro, rel, floor, what=name + " mixed residual")
-    r_only = es.residual_evaluate(xd)
-    assert torch.equal(r_only, rm)
+    r_only = es.residual_evaluate(xd)  # colour-ordered: the same sums as the coloured mixed assembly
+    if order == "coloured":
+        assert torch.equal(r_only, rm)
+    else:
+        assert_entrywise(r_only.cpu().numpy(), ro, rel, floor, what=name + " residual-only")
     S = np.abs(vo).max()
     err = np.abs(full[is_uu] - vo[is_uu]).max() / S
     assert err < MIXED_UU_TOL, (name, err)

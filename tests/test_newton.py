@@ -166,14 +166,16 @@ def test_line_search_backtracks_on_a_large_step(oracle):
 def test_failed_line_search_keeps_the_previous_state(oracle):
     """A line search that finds no step with sufficient decrease rejects the
     step: with alpha = 0.99 no trial step above ~0.02 passes on the nonlinear
-    stretch, and min_lambda = 0.3 stops the backtracking before that, so the
-    first Newton step fails; the state must be the one before the step and
+    stretch (for a Newton direction f(lam) ~ f0 (1 - lam)^2 must stay below
+    f0 (1 - 1.98 lam)), and min_lambda = 0.6 stops the backtracking after the
+    second trial (which is at most 0.5), so the first Newton step fails; the
+    state must be the one before the step and
     the report must say so (PETSc's bt line search leaves X unchanged on a
     failed reduction)."""
     m = quad_small()
     bc = N.clamped_stretch_shear_conditions(m, 1.3, 0.1)
     es = oracle.EquationsSet(m)
-    s = N.LoadStepSolver(es, bc, N.NewtonOptions(linear="dense", alpha=0.99, min_lambda=0.3), device="cpu")
+    s = N.LoadStepSolver(es, bc, N.NewtonOptions(linear="dense", alpha=0.99, min_lambda=0.6), device="cpu")
     x0 = s.apply_increment(torch.from_numpy(N.initial_state(m)), 1, 1)
     x, rep = s.newton(x0.clone())
     assert rep.line_search_failed and not rep.converged
@@ -392,8 +394,9 @@ def test_native_newton_rejects_inverted_initial_state(cuda):
 @pytest.mark.gpu
 @pytest.mark.parametrize("on_device", [True, False])
 def test_native_newton_failed_line_search_keeps_state(cuda, on_device):
-    """fe_newton_load_step with alpha = 0.99 and min_lambda = 0.3 on a large
-    stretch: the first line search fails, x comes back as the state before
+    """fe_newton_load_step with alpha = 0.99 and min_lambda = 0.6 on a large
+    stretch (see the CPU test above): the first line search fails after two
+    trials, x comes back as the state before
     the step (the Dirichlet values applied), line_search_failed is set and
     the step is not converged."""
     from cm_gb300 import FiniteElasticityEquationsSet
@@ -403,7 +406,7 @@ def test_native_newton_failed_line_search_keeps_state(cuda, on_device):
     x0 = N.initial_state(m)
     x0[bc.dofs] = bc.full
     x = torch.from_numpy(x0.copy()).cuda() if on_device else x0.copy()
-    rep = es.newton_load_step(x, bc.dofs, bc.full, alpha=0.99, min_lambda=0.3, ksp_rtol=1e-8)
+    rep = es.newton_load_step(x, bc.dofs, bc.full, alpha=0.99, min_lambda=0.6, ksp_rtol=1e-8)
     xr = x.cpu().numpy() if on_device else x
     assert rep["line_search_failed"] == 1 and rep["converged"] == 0
     assert rep["iterations"] == 1 and rep["residual_norm"] == rep["residual_norm_initial"]
