@@ -661,6 +661,55 @@ def loadstep_leg(dev, n=8, n_train=48, n_test=4, increments=8, modes=64, train_s
     }
 
 
+def config2_loading_leg(dev, increments=10, stretch=1.2, shear=0.1):
+    """The single-large-mesh configuration's loading: the 32^3 triquadratic
+    box (859,812 dofs) clamped at x = 0 and moved to stretch 1.2 / shear 0.1
+    on x = 1 in 10 load increments (the reference's fixed-incremented rule),
+    Newton from the reference guess (the current field) to ||r||_2 <= 1e-10
+    at every increment, three ways: the plain method (FP64 Jacobian, KSP
+    relative tolerance 1e-5, the reference default), the mixed Jacobian with
+    the same tolerance, and the mixed Jacobian with Eisenstat-Walker forcing.
+    The linear solver is GMRES with the multigrid block preconditioner in all
+    three."""
+    import torch
+
+    from cm_gb300 import FiniteElasticityEquationsSet
+    from cm_gb300 import newton as N
+    m, _, _ = config_mesh("cfg2")
+    es = FiniteElasticityEquationsSet(m)
+    bc = N.clamped_stretch_shear_conditions(m, stretch, shear)
+    arms = {"plain_fp64": N.NewtonOptions(linear="mg"),
+            "mixed": N.NewtonOptions(linear="mg", precision="mixed"),
+            "mixed_ew": N.NewtonOptions(linear="mg", precision="mixed", forcing="ew")}
+    out, xs = {}, {}
+    for name, opt in arms.items():
+        solver = N.LoadStepSolver(es, bc, opt, device=dev)
+        x0 = torch.from_numpy(N.initial_state(m)).to(dev)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        x, reps = solver.solve(x0, increments)
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter() - t0
+        xs[name] = x
+        out[name] = {"newton_iterations": int(sum(r.iterations for r in reps)),
+                     "krylov_iterations": int(sum(sum(r.linear_iterations) for r in reps)),
+                     "solve_ms": 1e3 * t, "load_step_ms": 1e3 * t / max(len(reps), 1),
+                     "increments_done": len(reps),
+                     "converged_1e-10": bool(all(r.converged for r in reps) and len(reps) == increments),
+                     "final_residual": float(reps[-1].residual_norms[-1]),
+                     "assembly_s": float(sum(r.assembly_seconds for r in reps)),
+                     "linear_s": float(sum(r.linear_seconds for r in reps))}
+        del solver
+        torch.cuda.empty_cache()
+    ref = xs["plain_fp64"]
+    for name in ("mixed", "mixed_ew"):
+        out[name]["max_solution_difference"] = float((xs[name] - ref).abs().max())
+    out["workload"] = ("32^3 triquadratic-u/trilinear-p box (%d dofs), MR c1=2 c2=6, x=0 clamped, x=1 moved to "
+                       "stretch %.2f + shear %.2f in %d increments" % (es.ndofs, stretch, shear, increments))
+    out["speedup_mixed_ew"] = out["plain_fp64"]["solve_ms"] / out["mixed_ew"]["solve_ms"]
+    return out
+
+
 def batch_arm(args):
     """Batched configuration: 256 independent box meshes assembled in one
     persistent launch (captured in a CUDA graph), launch shape from the
@@ -795,7 +844,14 @@ def main():
     ap.add_argument("--loadstep-increments", type=int, default=8, help="load increments of the plain method")
     ap.add_argument("--no-loadstep", dest="loadstep", action="store_false",
                     help="skip the Newton load-step comparison (plain FP64 vs mixed + learned warm start)")
+    ap.add_argument("--config2-loading", action="store_true",
+                    help="only solve the 32^3 box's 10-increment loading (plain FP64 vs mixed) and print it")
     args = ap.parse_args()
+    if args.config2_loading:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"config2_loading": config2_loading_leg(torch.device("cuda", 0))}))
+        return
     if args.impl == "reference":
         reference_arm(args)
     elif args.config == "cfg3":

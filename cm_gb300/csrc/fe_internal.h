@@ -109,6 +109,23 @@ struct StageOut {
   double* r;
 };
 
+// Arguments of the fused staged assembly (fe_mixed.cu): the incidence lists,
+// a work counter (next element group, zero before the launch), the per-row-
+// node counts of finished elements around the node (u nodes, then pressure
+// row nodes; zero before the launch), and the boundary-face masks when a
+// surface-pressure load is set (else NULL).
+struct FusedArgs {
+  const int32_t* u_inc_ptr;
+  const int32_t* u_inc;
+  const int32_t* p_inc_ptr;
+  const int32_t* p_inc;
+  int* work;
+  int* node_done;
+  const uint8_t* bmask;
+  int gwarps;  // warps that gather (set by the launcher)
+  int gbytes;  // scratch bytes per gathering warp (set by the launcher)
+};
+
 // Launches the mixed-precision assembly kernel for one colour (fe_mixed.cu),
 // with the high-precision phases in FP64 or in double-float arithmetic.
 // Returns a cudaError_t value.
@@ -119,6 +136,13 @@ int launch_mixed(const HostSetup& s, const KParams& kp, int num_sms, void* strea
 // one launch, without colour order.  Returns a cudaError_t value.
 int launch_mixed_staged(const HostSetup& s, const KParams& kp, const StageOut& so, int num_sms, void* stream,
                         bool double_float);
+
+// The staged assembly in one launch with the row gathers inside it
+// (fe_mixed.cu); fused_fits() says whether a mesh's largest row node fits the
+// kernel's gather scratch.  Returns a cudaError_t value.
+int fused_fits(const HostSetup& s);
+int launch_mixed_fused(const HostSetup& s, const KParams& kp, const StageOut& so, const FusedArgs& fa, int num_sms,
+                       void* stream, bool double_float);
 
 // Sums the staged element outputs into the CSR rows (uu FP32, coupling FP64)
 // and the residual, one row node at a time, in the fixed element order of

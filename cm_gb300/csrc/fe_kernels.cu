@@ -485,6 +485,7 @@ struct fe_equations_set {
   int32_t *d_u_inc_ptr = nullptr, *d_u_inc = nullptr, *d_p_inc_ptr = nullptr, *d_p_inc = nullptr;
   float* d_st_uu = nullptr;
   double *d_st_cp = nullptr, *d_st_r = nullptr;
+  int* d_fuse = nullptr;  // fused staged assembly: [0] work counter, [1 ..] per-row-node counts
   unsigned* d_status = nullptr;
   int32_t* d_col = nullptr;  // CSR columns on the device, uploaded on first use (Newton driver)
   // staging for calls given host memory
@@ -619,10 +620,31 @@ int mixed_staged(fe_handle h, const double* dx, float* du, double* dc, double* d
   kp.elems = nullptr;
   kp.first_elem = 0;
   kp.count = s.ne;
+  const int nb = s.bnd_ptr.empty() ? 0 : s.bnd_ptr[s.ncolours];
+  if (cmfe::fused_fits(s)) {
+    // one launch: element records and row gathers together
+    const size_t counters = 1 + (size_t)s.nu + (size_t)s.npn;
+    if ((rc = ensure((void**)&h->d_fuse, sizeof(int) * counters))) return rc;
+    CUDA_TRY(cudaMemsetAsync(h->d_fuse, 0, sizeof(int) * counters, st));
+    cmfe::FusedArgs fa;
+    std::memset(&fa, 0, sizeof(fa));
+    fa.u_inc_ptr = h->d_u_inc_ptr;
+    fa.u_inc = h->d_u_inc;
+    fa.p_inc_ptr = h->d_p_inc_ptr;
+    fa.p_inc = h->d_p_inc;
+    fa.work = h->d_fuse;
+    fa.node_done = h->d_fuse + 1;
+    fa.bmask = h->has_surfp && nb > 0 ? h->d_bnd_mask : nullptr;
+    const int e = cmfe::launch_mixed_fused(s, kp, so, fa, h->num_sms, st, double_float);
+    if (e != 0)
+      return set_error(FE_ERR_CUDA, std::string("fused kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+    h->launches += 1;
+    if (count) *count += 1;
+    return FE_NO_ERROR;
+  }
   int e = cmfe::launch_mixed_staged(s, kp, so, h->num_sms, st, double_float);
   if (e != 0) return set_error(FE_ERR_CUDA, std::string("staged kernel launch: ") + cudaGetErrorString((cudaError_t)e));
   int64_t n = 1;
-  const int nb = s.bnd_ptr.empty() ? 0 : s.bnd_ptr[s.ncolours];
   if (h->has_surfp && nb > 0) {
     e = cmfe::launch_surface(s, kp, h->d_bnd_elems, h->d_bnd_mask, nb, 2, 1, h->num_sms, st, so);
     if (e != 0) return set_error(FE_ERR_CUDA, std::string("surface kernel launch: ") + cudaGetErrorString((cudaError_t)e));
@@ -695,6 +717,21 @@ bool is_device_ptr(const void* p) {
     return false;
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Page-locked host memory that the device can address (cudaHostAlloc,
+// cudaHostRegister, or torch's pinned tensors): *dptr receives the address
+// kernels use for it (under unified addressing, the host address itself).
+bool mapped_host_ptr(const void* p, void** dptr) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+  *dptr = a.devicePointer;
+  return true;
 }
 
 int ensure(void** buf, size_t bytes) {
@@ -986,7 +1023,7 @@ int fe_destroy(fe_handle h) {
                   h->d_wp, h->d_elem_table, h->d_colour_elems, h->d_tables, h->d_geo, h->d_mat,
                   h->d_gbf_u, h->d_gbf_p, h->d_gw, h->d_status, h->s_x, h->s_r, h->s_vals, h->s_cp,
                   h->s_uu, h->s_elem, h->d_col, h->d_u_inc_ptr, h->d_u_inc, h->d_p_inc_ptr, h->d_p_inc,
-                  h->d_st_uu, h->d_st_cp, h->d_st_r};
+                  h->d_st_uu, h->d_st_cp, h->d_st_r, h->d_fuse};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete h;
@@ -1161,11 +1198,21 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
   bool hx;
   const double* dx;
   if ((rc = stage_in(h, x, &dx, st, &hx))) return rc;
-  const bool hu = !is_device_ptr(values_uu), hc = !is_device_ptr(values_coupling);
-  const bool hr = r && !is_device_ptr(r);
+  bool hu = !is_device_ptr(values_uu), hc = !is_device_ptr(values_coupling);
+  bool hr = r && !is_device_ptr(r);
   float* du = values_uu;
   double* dc = values_coupling;
   double* dr = r;
+  bool mapped_out = false;  // some output is host memory written in place: wait before returning
+  if (h->assembly_order == FE_ASSEMBLY_STAGED) {
+    // the row gather writes each output row once, contiguously: page-locked
+    // host outputs are written in place over the host link, with no device
+    // copy of the result and no separate device-to-host copy
+    void* p;
+    if (hu && mapped_host_ptr(values_uu, &p)) du = static_cast<float*>(p), hu = false, mapped_out = true;
+    if (hc && mapped_host_ptr(values_coupling, &p)) dc = static_cast<double*>(p), hc = false, mapped_out = true;
+    if (hr && mapped_host_ptr(r, &p)) dr = static_cast<double*>(p), hr = false, mapped_out = true;
+  }
   if (hu) {
     if ((rc = ensure((void**)&h->s_uu, sizeof(float) * h->hs.nnz_uu))) return rc;
     du = h->s_uu;
@@ -1183,7 +1230,7 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
   if (hu) CUDA_TRY(cudaMemcpyAsync(values_uu, du, sizeof(float) * h->hs.nnz_uu, cudaMemcpyDeviceToHost, st));
   if (hc) CUDA_TRY(cudaMemcpyAsync(values_coupling, dc, sizeof(double) * h->hs.nnz_cp, cudaMemcpyDeviceToHost, st));
   if (hr) CUDA_TRY(cudaMemcpyAsync(r, dr, sizeof(double) * h->hs.ndofs, cudaMemcpyDeviceToHost, st));
-  if (hu || hc || hr) return finish_status(h, st);
+  if (hu || hc || hr || mapped_out) return finish_status(h, st);
   return FE_NO_ERROR;
 }
 

@@ -76,17 +76,22 @@ struct MixCfg {
   static constexpr int O_W = align16(O_L + 6 * 8);
   static constexpr int O_1D = align16(O_W + NG * 8);
   static constexpr int O_LM = align16(O_1D + 6 * N1 * 8);  // L x (1-D value | derivative) products
-  static constexpr int O_Z = align16(O_LM + 12 * N1 * 8);
+  // constant tables first, then the per-group scratch from O_Z on (the fused
+  // kernel reuses the scratch between groups for its row gathers)
+  static constexpr int O_PHI32 = align16(O_LM + 12 * N1 * 8);
+  static constexpr int O_A = align16(O_PHI32 + NG * PHS * 4);
+  static constexpr int O_Z = align16(O_A + 2 * AROWS * KPW * 4);
   static constexpr int O_P = align16(O_Z + EG * 3 * NPE * 8);
   static constexpr int O_DZ = align16(O_P + EG * 8 * 8);
   static constexpr int O_PG = align16(O_DZ + EG * NG * 9 * 8);
   static constexpr int O_R64 = align16(O_PG + EG * NG * 8);
-  static constexpr int O_PHI32 = align16(O_R64 + EG * NG * REC64 * 8);
-  static constexpr int O_R32 = align16(O_PHI32 + NG * PHS * 4);
-  static constexpr int O_A = align16(O_R32 + EG * NG * REC32 * 4);
-  static constexpr int O_F32 = align16(O_A + 2 * AROWS * KPW * 4);
+  static constexpr int O_R32 = align16(O_R64 + EG * NG * REC64 * 8);
+  static constexpr int O_F32 = align16(O_R32 + EG * NG * REC32 * 4);
   static constexpr int O_NODE = align16(O_F32 + EG * NG * 24 * 4);
   static constexpr int SMEM = align16(O_NODE + EG * (NR + 1) * 4);
+  static constexpr int O_SCRATCH = O_Z;
+  // fused kernel: the list of row nodes a group completed, just below O_NODE
+  static constexpr int O_READY = O_NODE - align16(EG * NR * 4);
 };
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {

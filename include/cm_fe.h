@@ -132,7 +132,12 @@ int fe_jacobian_evaluate(fe_handle h, const double* x, double* values, double* r
  * pressure-pressure block) in FP64.  The two value arrays follow the split
  * pattern returned by fe_mixed_layout().  If r is not NULL the FP64 residual
  * at x is produced by the same pass.  No counterpart in the reference (which
- * assembles in FP64 only); its FP64 parts match fe_jacobian_evaluate. */
+ * assembles in FP64 only); its FP64 parts match fe_jacobian_evaluate.  In
+ * the staged assembly order (fe_set_assembly_order), outputs in page-locked
+ * host memory (cudaHostAlloc / cudaHostRegister) are written in place by the
+ * row gather over the host link, without a device copy of the result; other
+ * host memory goes through staging buffers.  Either way the call returns
+ * after the host outputs are written. */
 int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, double* values_coupling,
                                double* r, void* stream);
 

@@ -165,17 +165,18 @@ def test_line_search_backtracks_on_a_large_step(oracle):
 
 def test_failed_line_search_keeps_the_previous_state(oracle):
     """A line search that finds no step with sufficient decrease rejects the
-    step: with alpha = 0.99 no trial step above ~0.02 passes on the nonlinear
-    stretch (for a Newton direction f(lam) ~ f0 (1 - lam)^2 must stay below
-    f0 (1 - 1.98 lam)), and min_lambda = 0.6 stops the backtracking after the
-    second trial (which is at most 0.5), so the first Newton step fails; the
-    state must be the one before the step and
-    the report must say so (PETSc's bt line search leaves X unchanged on a
-    failed reduction)."""
+    step.  The step is capped at max_step = 1e-9, so along it f = 1/2 ||r||^2
+    changes by lam * slope to first order (slope = r . (J d), the directional
+    derivative, whatever the accuracy of the linear solve), and with
+    alpha = 1.5 the sufficient-decrease bound f0 + 1.5 lam slope lies below
+    that for every descent direction: no trial passes, and min_lambda = 0.6
+    stops the backtracking after its second trial.  The state must be the
+    one before the step and the report must say so (PETSc's bt line search
+    leaves X unchanged on a failed reduction)."""
     m = quad_small()
     bc = N.clamped_stretch_shear_conditions(m, 1.3, 0.1)
     es = oracle.EquationsSet(m)
-    s = N.LoadStepSolver(es, bc, N.NewtonOptions(linear="dense", alpha=0.99, min_lambda=0.6), device="cpu")
+    s = N.LoadStepSolver(es, bc, N.NewtonOptions(linear="dense", alpha=1.5, min_lambda=0.6, max_step=1e-9), device="cpu")
     x0 = s.apply_increment(torch.from_numpy(N.initial_state(m)), 1, 1)
     x, rep = s.newton(x0.clone())
     assert rep.line_search_failed and not rep.converged
@@ -394,11 +395,11 @@ def test_native_newton_rejects_inverted_initial_state(cuda):
 @pytest.mark.gpu
 @pytest.mark.parametrize("on_device", [True, False])
 def test_native_newton_failed_line_search_keeps_state(cuda, on_device):
-    """fe_newton_load_step with alpha = 0.99 and min_lambda = 0.6 on a large
-    stretch (see the CPU test above): the first line search fails after two
-    trials, x comes back as the state before
-    the step (the Dirichlet values applied), line_search_failed is set and
-    the step is not converged."""
+    """fe_newton_load_step with alpha = 1.5, min_lambda = 0.6 and
+    max_step = 1e-9 (see the CPU test above): the first line search fails
+    after two trials, x comes back as the state before the step (the
+    Dirichlet values applied), line_search_failed is set and the step is not
+    converged."""
     from cm_gb300 import FiniteElasticityEquationsSet
     m = quad_small()
     bc = N.clamped_stretch_shear_conditions(m, 1.3, 0.1)
@@ -406,7 +407,7 @@ def test_native_newton_failed_line_search_keeps_state(cuda, on_device):
     x0 = N.initial_state(m)
     x0[bc.dofs] = bc.full
     x = torch.from_numpy(x0.copy()).cuda() if on_device else x0.copy()
-    rep = es.newton_load_step(x, bc.dofs, bc.full, alpha=0.99, min_lambda=0.6, ksp_rtol=1e-8)
+    rep = es.newton_load_step(x, bc.dofs, bc.full, alpha=1.5, min_lambda=0.6, max_step=1e-9, ksp_rtol=1e-8)
     xr = x.cpu().numpy() if on_device else x
     assert rep["line_search_failed"] == 1 and rep["converged"] == 0
     assert rep["iterations"] == 1 and rep["residual_norm"] == rep["residual_norm_initial"]
