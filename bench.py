@@ -463,11 +463,12 @@ def our_arm(args):
         dist.destroy_process_group()
 
 
-def slab_variants_leg(dev, steps, n=32, ex=32, ey=32, ez=8):
-    """Material / pressure variants of the slab assembled together: n slabs
-    (C log-uniform in [0.5, 2] kPa, cavity pressure uniform in [0.25, 2] kPa
-    on z = 0) in one persistent launch per assembly, replayed from a CUDA
-    graph with the autotuned launch shape."""
+def slab_variants_leg(dev, steps, n=32, ex=64, ey=64, ez=16):
+    """Material / pressure variants of the slab assembled together: n
+    variants of one slab geometry (C log-uniform in [0.5, 2] kPa, cavity
+    pressure uniform in [0.25, 2] kPa on z = 0; fe_clone shares the mesh
+    arrays) in one batched call per assembly, replayed from a CUDA graph with
+    the autotuned launch shape."""
     import numpy as np
     import torch
 
@@ -477,10 +478,11 @@ def slab_variants_leg(dev, steps, n=32, ex=32, ey=32, ez=8):
     from cm_gb300.warmstart import sample_slab_parameters
     params = sample_slab_parameters(n, seed=51)
     t0 = time.perf_counter()
+    m = M.guccione_slab(ex, ey, ez, seed=0)
+    base = FiniteElasticityEquationsSet(m)
     meshes, sets, xs = [], [], []
     for i, (p, c) in enumerate(params):
-        m = M.guccione_slab(ex, ey, ez, materials=(float(c), 18.5, 3.58, 1.63), seed=i)
-        es = FiniteElasticityEquationsSet(m)
+        es = base.clone(np.array([float(c), 18.5, 3.58, 1.63]))
         es.set_surface_pressure(bottom_face_pressure(m, float(p)))
         meshes.append(m)
         sets.append(es)
@@ -519,8 +521,9 @@ def slab_variants_leg(dev, steps, n=32, ex=32, ey=32, ez=8):
     t_sep = a.elapsed_time(b) / 1e3 / steps
     ne = sum(m.ne for m in meshes)
     B = sum(algorithmic_bytes(m, s_, True) for m, s_ in zip(meshes, sets))
-    return {"workload": "%d Guccione slabs %dx%dx%d triquadratic (C log-U[0.5,2] kPa, cavity pressure U[0.25,2] kPa), "
-                        "one persistent launch per assembly of all of them, from a CUDA graph" % (n, ex, ey, ez),
+    return {"workload": "%d variants of the %dx%dx%d triquadratic Guccione slab (C log-U[0.5,2] kPa, cavity pressure "
+                        "U[0.25,2] kPa), one batched call per assembly of all of them, from a CUDA graph"
+                        % (n, ex, ey, ez),
             "elements": ne, "value": ne / t, "unit": UNIT, "ms_per_step": 1e3 * t, "graph_replays_per_step": 1,
             "kernel_launches_per_step": launches,
             "roofline_frac_hbm": B / t / 1e9 / peaks()["hbm_gbs"], "autotuned": cfg, "setup_s": setup_s,
@@ -710,6 +713,110 @@ def config2_loading_leg(dev, increments=10, stretch=1.2, shear=0.1):
     return out
 
 
+def config4_study(dev, n=16, n_train=2048, n_test=256, n_timed=32, increments=10, modes=64, train_steps=4000):
+    """The learned-warm-start configuration at its stated size: the 16^3
+    triquadratic box (112,724 dofs), 2,048 training and 256 held-out
+    parameter sets (stretch, shear, c1, c2) from the configuration's
+    distributions, 64 POD modes, the 4-256-256-256-64 network.
+
+    Training states are Newton solves to ||r||_2 <= 1e-10 with the mixed
+    Jacobian and Eisenstat-Walker forcing (arm (iii)'s solver), each started
+    from the previous training solution along a nearest-neighbour path in
+    parameter space (one full-load increment, the reference increments where
+    that fails): they are the converged solutions whatever the start or the
+    Jacobian precision (arms (i) and (iii) agree to 2e-10).  Four arms on held-out problems, each to ||r||_2 <= 1e-10:
+      (i)   plain: FP64 Jacobian, reference guess, `increments` increments,
+            KSP relative tolerance 1e-5 (the reference default);
+      (ii)  (i) with Eisenstat-Walker forcing;
+      (iii) mixed Jacobian, Eisenstat-Walker, reference guess and increments;
+      (iv)  mixed Jacobian, Eisenstat-Walker, the learned guess in one
+            increment (arm (iii) as the fallback).
+    Arm (iv) runs on all held-out problems; arms (i)-(iii) on the first
+    `n_timed` of them (the same problems), which the ratios use."""
+    import numpy as np
+    import torch
+
+    from cm_gb300 import FiniteElasticityEquationsSet
+    from cm_gb300 import mesh as M
+    from cm_gb300 import newton as N
+    from cm_gb300 import warmstart as W
+    t_all = time.perf_counter()
+    m = M.regular_box(n, n, n, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0), perturb=0.1, seed=2)
+    es = FiniteElasticityEquationsSet(m)
+    arms = {
+        "i_plain": W.ParametricProblem(es, N.NewtonOptions(linear="mg"), device=dev),
+        "ii_plain_ew": W.ParametricProblem(es, N.NewtonOptions(linear="mg", forcing="ew"), device=dev),
+        "iii_mixed_ew": W.ParametricProblem(es, N.NewtonOptions(linear="mg", precision="mixed", forcing="ew"),
+                                            device=dev),
+    }
+    learned = arms["iii_mixed_ew"]
+    train = W.sample_parameters(n_train, seed=21)
+    test = W.sample_parameters(n_test, seed=22)
+    t0 = time.perf_counter()
+    states, it_train = W.generate_solves(learned, train, increments, continuation=True)
+    t_data = time.perf_counter() - t0
+    ws = W.LearnedWarmStart(learned.n_pressure, modes=min(modes, n_train - 1), seed=0, device=dev)
+    rep = ws.fit(train, states, steps=train_steps, lr=2e-3, batch=256)
+    del states
+    # warm-up of every path
+    for a in arms.values():
+        a.solve_reference(test[0], increments)
+    learned.solve_from_state(test[0], ws.predict(test[:1])[0], increments)
+
+    def summary(rows):
+        k = len(rows)
+        return {"problems": k,
+                "newton_iterations": float(np.mean([r["newton"] for r in rows])),
+                "krylov_iterations": float(np.mean([r["krylov"] for r in rows])),
+                "solve_ms": 1e3 * float(np.mean([r["s"] for r in rows])),
+                "load_step_ms": 1e3 * float(np.mean([r["s"] / r["incs"] for r in rows])),
+                "all_converged_1e-10": bool(all(r["ok"] for r in rows))}
+
+    def row(x, reps, t):
+        return {"newton": sum(r.iterations for r in reps), "krylov": sum(sum(r.linear_iterations) for r in reps),
+                "s": t, "incs": len(reps), "x": x,
+                "ok": bool(reps[-1].converged and reps[-1].residual_norms[-1] <= 1e-10)}
+
+    out = {}
+    ref_x = []
+    for name, a in arms.items():
+        rows = []
+        for p in test[:n_timed]:
+            x, reps, t = a.solve_reference(p, increments)
+            rows.append(row(x, reps, t))
+        if name == "i_plain":
+            ref_x = [r["x"] for r in rows]
+        out[name] = summary(rows)
+        out[name]["max_difference_to_i"] = float(max((r["x"] - xr).abs().max() for r, xr in zip(rows, ref_x)))
+    rows, accepted = [], 0
+    for p in test:
+        t1 = time.perf_counter()
+        guess = ws.predict(p[None])[0]
+        x, reps, _, ok = learned.solve_from_state(p, guess, increments)
+        t = time.perf_counter() - t1
+        accepted += int(ok)
+        rows.append(row(x, reps, t))
+        rows[-1]["incs"] = 1
+    out["iv_mixed_ew_learned"] = summary(rows)
+    out["iv_mixed_ew_learned"]["accepted_guesses"] = accepted
+    out["iv_mixed_ew_learned"]["max_difference_to_i"] = float(
+        max((r["x"] - xr).abs().max() for r, xr in zip(rows[:n_timed], ref_x)))
+    iv_timed = summary(rows[:n_timed])
+    out["iv_on_timed_problems"] = iv_timed
+    for name in ("i_plain", "ii_plain_ew", "iii_mixed_ew"):
+        out["speedup_iv_vs_" + name] = out[name]["solve_ms"] / iv_timed["solve_ms"]
+    out["workload"] = ("%d^3 triquadratic-u/trilinear-p box (%d dofs), clamped stretch U[1,1.3] + shear U[0,0.2], "
+                       "MR c1,c2 log-U[0.5,10]; %d training, %d held-out problems (%d timed on every arm)"
+                       % (n, es.ndofs, n_train, n_test, n_timed))
+    out["training"] = {"solves": n_train, "data_s": t_data, "mean_newton_iterations": float(it_train.mean()),
+                       "modes": rep.modes, "pod_energy": rep.energy, "pod_relative_error": rep.pod_relative_error,
+                       "train_loss": rep.train_loss, "train_s": rep.seconds, "steps": train_steps,
+                       "data": "Newton to 1e-10 (mixed Jacobian, Eisenstat-Walker), continuation along a "
+                               "nearest-neighbour path"}
+    out["total_s"] = time.perf_counter() - t_all
+    return out
+
+
 def batch_arm(args):
     """Batched configuration: 256 independent box meshes assembled in one
     persistent launch (captured in a CUDA graph), launch shape from the
@@ -846,7 +953,19 @@ def main():
                     help="skip the Newton load-step comparison (plain FP64 vs mixed + learned warm start)")
     ap.add_argument("--config2-loading", action="store_true",
                     help="only solve the 32^3 box's 10-increment loading (plain FP64 vs mixed) and print it")
+    ap.add_argument("--config4-study", action="store_true",
+                    help="only run the learned-warm-start configuration at its stated size (2,048 training, "
+                         "256 held-out solves of the 16^3 box, four arms) and print it")
+    ap.add_argument("--config4-train", type=int, default=2048)
+    ap.add_argument("--config4-test", type=int, default=256)
+    ap.add_argument("--config4-timed", type=int, default=32)
     args = ap.parse_args()
+    if args.config4_study:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"config4_study": config4_study(torch.device("cuda", 0), n_train=args.config4_train,
+                                                         n_test=args.config4_test, n_timed=args.config4_timed)}))
+        return
     if args.config2_loading:
         import torch
         torch.cuda.set_device(0)

@@ -84,6 +84,7 @@ SIGNATURES = {
     "fe_element_jacobians": [_vp, _vp, _i32, _i32, _vp, _vp],
     "fe_set_high_precision": [_vp, _i32],
     "fe_set_assembly_order": [_vp, _i32],
+    "fe_clone": [_vp, C.POINTER(_vp)],
     "fe_set_surface_pressure": [_vp, _vp],
     "fe_set_materials": [_vp, _vp],
     "fe_newton_options_default": [C.POINTER(FENewtonOptions)],

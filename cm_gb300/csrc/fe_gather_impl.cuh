@@ -40,12 +40,53 @@ __device__ __forceinline__ T rec_load(const T* p) {
     return *p;
 }
 
+// Drops the records of element e from L2 without writing them back (every
+// row node of the element has been gathered, so no one reads them again in
+// this assembly, and the next assembly rewrites them): the records are lines
+// of 128 bytes each (line-aligned strides), discarded by one warp.
+template <int NPE, int NPP>
+__device__ __forceinline__ void discard_records(const cmfe::StageOut& S, int e, int lane) {
+  constexpr int LU = cmfe::rec_stride_uu(NPE) * 4 / 128, LC = cmfe::rec_stride_cp(NPE, NPP) * 8 / 128,
+                LR = cmfe::rec_stride_r(NPE, NPP) * 8 / 128;
+  const char* u = reinterpret_cast<const char*>(S.uu + (size_t)e * cmfe::rec_stride_uu(NPE));
+  const char* c = reinterpret_cast<const char*>(S.cp + (size_t)e * cmfe::rec_stride_cp(NPE, NPP));
+  const char* r = reinterpret_cast<const char*>(S.r + (size_t)e * cmfe::rec_stride_r(NPE, NPP));
+  for (int i = lane; i < LU + LC + LR; i += 32) {
+    const char* p = i < LU ? u + 128 * i : (i < LU + LC ? c + 128 * (i - LU) : r + 128 * (i - LU - LC));
+    asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
+  }
+}
+
+// Counts one more gathered row node for every element around a node (the
+// incidences k0 .. k1 - 1 of the packed list, element = packed >> shift) and
+// drops the records of those elements whose row nodes are all gathered.
+template <int NPE, int NPP>
+__device__ __forceinline__ void release_elements(const cmfe::StageOut& S, int* elem_done, const int32_t* inc, int k0,
+                                                 int k1, int shift, int lane) {
+  constexpr int NR = NPE + NPP;
+  for (int kb = k0; kb < k1; kb += 32) {
+    const int k = kb + lane;
+    bool last = false;
+    int e = 0;
+    if (k < k1) {
+      e = inc[k] >> shift;
+      last = atomicAdd(elem_done + e, 1) + 1 == NR;
+    }
+    unsigned m = __ballot_sync(0xffffffffu, last);
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      discard_records<NPE, NPP>(S, __shfl_sync(0xffffffffu, e, src), lane);
+    }
+  }
+}
+
 // The three displacement rows of u node a, by one warp; `mine` is the warp's
 // shared scratch (36 wu bytes rounded up to 16, then 24 wc bytes).
 template <int NPE, int NPP, bool CG>
 __device__ __forceinline__ void gather_unode(const cmfe::KParams& P, const cmfe::StageOut& S, const int32_t* u_inc_ptr,
                                              const int32_t* u_inc, int a, unsigned char* mine, int lane) {
-  constexpr int NR = NPE + NPP, NU3 = 3 * NPE, NROW = NU3 + NPP;
+  constexpr int NR = NPE + NPP, NU3 = 3 * NPE;
   const int nu = P.nu;
   const int wu = P.wu[a];
   const int ru = 3 * wu;  // uu row length
@@ -63,7 +104,7 @@ __device__ __forceinline__ void gather_unode(const cmfe::KParams& P, const cmfe:
     const uint16_t* tab = P.tables + ((size_t)P.elem_table[e] * NR + la) * NR;
     if (lane < NPE) {
       const int rk = tab[lane] & 0x7fff;
-      const float* src = S.uu + (size_t)e * NU3 * NU3 + (size_t)la * NU3 + lane;
+      const float* src = S.uu + (size_t)e * cmfe::rec_stride_uu(NPE) + (size_t)la * NU3 + lane;
       float v[9];
 #pragma unroll
       for (int m = 0; m < 3; ++m)
@@ -76,11 +117,11 @@ __device__ __forceinline__ void gather_unode(const cmfe::KParams& P, const cmfe:
     }
     if (lane < NPP) {
       const int rq = tab[NPE + lane] & 0x7fff;
-      const double* src = S.cp + ((size_t)e * NPP + lane) * NU3 + la;
+      const double* src = S.cp + (size_t)e * cmfe::rec_stride_cp(NPE, NPP) + lane * NU3 + la;
 #pragma unroll
       for (int m = 0; m < 3; ++m) acc_c[m * wc + rq] += rec_load<CG>(src + m * NPE);
     }
-    if (lane < 3 && P.r) racc += rec_load<CG>(S.r + (size_t)e * NROW + lane * NPE + la);
+    if (lane < 3 && P.r) racc += rec_load<CG>(S.r + (size_t)e * cmfe::rec_stride_r(NPE, NPP) + lane * NPE + la);
     __syncwarp();
   }
 #pragma unroll
@@ -98,7 +139,7 @@ __device__ __forceinline__ void gather_unode(const cmfe::KParams& P, const cmfe:
 template <int NPE, int NPP, bool CG>
 __device__ __forceinline__ void gather_pnode(const cmfe::KParams& P, const cmfe::StageOut& S, const int32_t* p_inc_ptr,
                                              const int32_t* p_inc, int q, unsigned char* mine, int lane) {
-  constexpr int NR = NPE + NPP, NU3 = 3 * NPE, NROW = NU3 + NPP;
+  constexpr int NR = NPE + NPP, NU3 = 3 * NPE;
   const size_t row = (size_t)3 * P.nu + q;
   const int wp = P.wp[q];
   const int len = P.cp_row_ptr[row + 1] - P.cp_row_ptr[row];
@@ -113,14 +154,14 @@ __device__ __forceinline__ void gather_pnode(const cmfe::KParams& P, const cmfe:
     if (lane < NPE) {
       const uint16_t* tab = P.tables + ((size_t)P.elem_table[e] * NR + NPE + lq) * NR;
       const int rk = tab[lane] & 0x7fff;
-      const double* src = S.cp + ((size_t)e * NPP + lq) * NU3 + lane;
+      const double* src = S.cp + (size_t)e * cmfe::rec_stride_cp(NPE, NPP) + lq * NU3 + lane;
       double v[3];
 #pragma unroll
       for (int n = 0; n < 3; ++n) v[n] = rec_load<CG>(src + n * NPE);
 #pragma unroll
       for (int n = 0; n < 3; ++n) acc[n * wp + rk] += v[n];
     }
-    if (lane == 0 && P.r) racc += rec_load<CG>(S.r + (size_t)e * NROW + NU3 + lq);
+    if (lane == 0 && P.r) racc += rec_load<CG>(S.r + (size_t)e * cmfe::rec_stride_r(NPE, NPP) + NU3 + lq);
     __syncwarp();
   }
   double* dc = P.vals + P.cp_row_ptr[row];

@@ -17,7 +17,7 @@ constexpr int NG = 27;  // 3x3x3 Gauss-Legendre points per element
 // first touched by the threads that fill them).
 template <class T>
 struct RawArray {
-  std::unique_ptr<T[]> p;
+  std::shared_ptr<T[]> p;  // shared by copies (handles cloned from one set-up)
   size_t n = 0;
   void allocate(size_t count) {
     p.reset(new T[count]);
@@ -61,8 +61,9 @@ struct HostSetup {
   // node (sorted by element number, packed e * 32 + local node) and around
   // every pressure row node (e * 8 + local pressure node).
   std::vector<int32_t> u_inc_ptr, u_inc, p_inc_ptr, p_inc;
-  // shared memory one gather warp needs: the larger of a u node's three rows
-  // (3 x 3 wu FP32, then 3 x its pressure columns FP64) and a pressure row (FP64)
+  // shared memory one gather warp needs (its incidence record and inverse
+  // rank maps); 0 when some row node has more than 32 elements around it, in
+  // which case the mixed assembly runs in colour order
   int gather_bytes = 0;
 };
 
@@ -99,10 +100,24 @@ struct KParams {
   unsigned* status;
 };
 
+#ifdef __CUDACC__
+#define CMFE_HD __host__ __device__
+#else
+#define CMFE_HD
+#endif
+
+// Strides of the per-element records of the staged assembly, in elements of
+// each record's type, rounded up to whole 128-byte lines so that the fused
+// kernel can drop a consumed record from L2 line by line without touching a
+// neighbour's (npe u nodes and npp pressure parameters per element).
+CMFE_HD constexpr int rec_stride_uu(int npe) { return (9 * npe * npe + 31) / 32 * 32; }          // floats
+CMFE_HD constexpr int rec_stride_cp(int npe, int npp) { return (npp * 3 * npe + 15) / 16 * 16; }  // doubles
+CMFE_HD constexpr int rec_stride_r(int npe, int npp) { return (3 * npe + npp + 15) / 16 * 16; }   // doubles
+
 // Per-element records of the staged assembly (mixed kernel with staged
 // output, surface mode 2, row gather): the full displacement block
-// [e][3 NPE][3 NPE] (FP32, row-major), the pressure-coupling rows
-// [e][NPP][3 NPE] and the residual [e][nrow] (FP64).
+// [3 NPE][3 NPE] (FP32, row-major), the pressure-coupling rows [NPP][3 NPE]
+// and the residual [nrow] (FP64) of element e, at e times the strides above.
 struct StageOut {
   float* uu;
   double* cp;
@@ -121,6 +136,7 @@ struct FusedArgs {
   const int32_t* p_inc;
   int* work;
   int* node_done;
+  int* elem_done;  // per element: how many of its row nodes are gathered (zero before the launch)
   const uint8_t* bmask;
   int gwarps;  // warps that gather (set by the launcher)
   int gbytes;  // scratch bytes per gathering warp (set by the launcher)

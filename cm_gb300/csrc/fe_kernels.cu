@@ -27,6 +27,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <string>
@@ -464,8 +465,20 @@ int dev_upload(T** dst, const std::vector<T>& src) {
 
 }  // namespace
 
+// Device arrays that depend only on the mesh (connectivity, pattern, rank
+// tables, geometry cache, quadrature, colouring, incidence lists): owned
+// together and shared by the handles fe_clone makes from one set-up.
+struct SharedDeviceSetup {
+  std::vector<void*> ptrs;
+  ~SharedDeviceSetup() {
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+  }
+};
+
 struct fe_equations_set {
   HostSetup hs;
+  std::shared_ptr<SharedDeviceSetup> shared;
   int device = 0;
   int num_sms = 0;
   int32_t *d_elem_u = nullptr, *d_elem_p = nullptr, *d_row_ptr = nullptr, *d_uu_row_ptr = nullptr,
@@ -605,11 +618,10 @@ int ensure(void** buf, size_t bytes);
 int mixed_staged(fe_handle h, const double* dx, float* du, double* dc, double* dr, bool double_float,
                  cudaStream_t st, int64_t* count) {
   const auto& s = h->hs;
-  const size_t nu3 = 3 * (size_t)s.npe;
   int rc;
-  if ((rc = ensure((void**)&h->d_st_uu, sizeof(float) * nu3 * nu3 * s.ne)) ||
-      (rc = ensure((void**)&h->d_st_cp, sizeof(double) * s.npp * nu3 * s.ne)) ||
-      (rc = ensure((void**)&h->d_st_r, sizeof(double) * s.nrow * (size_t)s.ne)))
+  if ((rc = ensure((void**)&h->d_st_uu, sizeof(float) * cmfe::rec_stride_uu(s.npe) * (size_t)s.ne)) ||
+      (rc = ensure((void**)&h->d_st_cp, sizeof(double) * cmfe::rec_stride_cp(s.npe, s.npp) * (size_t)s.ne)) ||
+      (rc = ensure((void**)&h->d_st_r, sizeof(double) * cmfe::rec_stride_r(s.npe, s.npp) * (size_t)s.ne)))
     return rc;
   KParams kp = base_params(h);
   kp.x = dx;
@@ -623,7 +635,7 @@ int mixed_staged(fe_handle h, const double* dx, float* du, double* dc, double* d
   const int nb = s.bnd_ptr.empty() ? 0 : s.bnd_ptr[s.ncolours];
   if (cmfe::fused_fits(s)) {
     // one launch: element records and row gathers together
-    const size_t counters = 1 + (size_t)s.nu + (size_t)s.npn;
+    const size_t counters = 1 + (size_t)s.nu + (size_t)s.npn + (size_t)s.ne;
     if ((rc = ensure((void**)&h->d_fuse, sizeof(int) * counters))) return rc;
     CUDA_TRY(cudaMemsetAsync(h->d_fuse, 0, sizeof(int) * counters, st));
     cmfe::FusedArgs fa;
@@ -634,6 +646,7 @@ int mixed_staged(fe_handle h, const double* dx, float* du, double* dc, double* d
     fa.p_inc = h->d_p_inc;
     fa.work = h->d_fuse;
     fa.node_done = h->d_fuse + 1;
+    fa.elem_done = h->d_fuse + 1 + s.nu + s.npn;
     fa.bmask = h->has_surfp && nb > 0 ? h->d_bnd_mask : nullptr;
     const int e = cmfe::launch_mixed_fused(s, kp, so, fa, h->num_sms, st, double_float);
     if (e != 0)
@@ -681,7 +694,8 @@ int mixed_colours(fe_handle h, const double* dx, float* du, double* dc, double* 
 // The mixed assembly in the handle's assembly order.
 int mixed_assemble(fe_handle h, const double* dx, float* du, double* dc, double* dr, bool double_float,
                    cudaStream_t st, int64_t* count) {
-  if (h->assembly_order == FE_ASSEMBLY_STAGED) return mixed_staged(h, dx, du, dc, dr, double_float, st, count);
+  if (h->assembly_order == FE_ASSEMBLY_STAGED && h->hs.gather_bytes > 0)
+    return mixed_staged(h, dx, du, dc, dr, double_float, st, count);
   return mixed_colours(h, dx, du, dc, dr, double_float, st, count);
 }
 
@@ -953,6 +967,15 @@ int device_pattern(fe_handle h, const int32_t** row_ptr, const int32_t** col, in
 }
 }  // namespace cmfe
 
+namespace {
+// The mesh-only device arrays of a handle (shared with its clones).
+std::vector<void*> shared_arrays(fe_handle h) {
+  return {h->d_bnd_elems, h->d_bnd_mask, h->d_geo_dd, h->d_elem_u, h->d_elem_p, h->d_row_ptr, h->d_uu_row_ptr,
+          h->d_cp_row_ptr, h->d_wu, h->d_wp, h->d_elem_table, h->d_colour_elems, h->d_tables, h->d_geo,
+          h->d_gbf_u, h->d_gbf_p, h->d_gw, h->d_u_inc_ptr, h->d_u_inc, h->d_p_inc_ptr, h->d_p_inc};
+}
+}  // namespace
+
 extern "C" {
 
 int fe_last_error(char* buf, int32_t size) {
@@ -1002,6 +1025,11 @@ int fe_create(const fe_mesh_desc* desc, fe_handle* out) {
   if ((rc = dev_upload(&h->d_u_inc_ptr, s.u_inc_ptr)) || (rc = dev_upload(&h->d_u_inc, s.u_inc)) ||
       (rc = dev_upload(&h->d_p_inc_ptr, s.p_inc_ptr)) || (rc = dev_upload(&h->d_p_inc, s.p_inc)))
     return fail(rc);
+  {
+    auto owner = std::make_shared<SharedDeviceSetup>();
+    owner->ptrs = shared_arrays(h);
+    h->shared = owner;
+  }
   if (cudaMalloc(&h->d_status, sizeof(unsigned)) != cudaSuccess ||
       cudaMemset(h->d_status, 0, sizeof(unsigned)) != cudaSuccess)
     return fail(set_error(FE_ERR_CUDA, "status allocation failed"));
@@ -1019,14 +1047,74 @@ int fe_create(const fe_mesh_desc* desc, fe_handle* out) {
 
 int fe_destroy(fe_handle h) {
   if (!h) return FE_NO_ERROR;
-  void* ptrs[] = {h->d_surfp, h->d_bnd_elems, h->d_bnd_mask, h->d_geo_dd, h->d_elem_u, h->d_elem_p, h->d_row_ptr, h->d_uu_row_ptr, h->d_cp_row_ptr, h->d_wu,
-                  h->d_wp, h->d_elem_table, h->d_colour_elems, h->d_tables, h->d_geo, h->d_mat,
-                  h->d_gbf_u, h->d_gbf_p, h->d_gw, h->d_status, h->s_x, h->s_r, h->s_vals, h->s_cp,
-                  h->s_uu, h->s_elem, h->d_col, h->d_u_inc_ptr, h->d_u_inc, h->d_p_inc_ptr, h->d_p_inc,
-                  h->d_st_uu, h->d_st_cp, h->d_st_r, h->d_fuse};
-  for (void* p : ptrs)
+  if (!h->shared) {  // a handle whose creation failed part-way owns what it uploaded
+    for (void* p : shared_arrays(h))
+      if (p) cudaFree(p);
+  }
+  // per-handle state: materials, surface load, status word, staging and records
+  void* own[] = {h->d_surfp, h->d_mat, h->d_status, h->s_x, h->s_r, h->s_vals, h->s_cp, h->s_uu, h->s_elem,
+                 h->d_col, h->d_st_uu, h->d_st_cp, h->d_st_r, h->d_fuse};
+  for (void* p : own)
     if (p) cudaFree(p);
-  delete h;
+  delete h;  // releases this handle's share of the mesh arrays
+  return FE_NO_ERROR;
+}
+
+int fe_clone(fe_handle src, fe_handle* out) {
+  if (!out) return set_error(FE_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  int rc = check_handle(src);
+  if (rc) return rc;
+  fe_handle h = new (std::nothrow) fe_equations_set();
+  if (!h) return set_error(FE_ERR_OUT_OF_MEMORY, "host allocation failed");
+  {
+    std::lock_guard<std::mutex> lk(src->mu);
+    h->hs = src->hs;  // vectors copied; the CSR column array is shared
+    h->shared = src->shared;
+    h->device = src->device;
+    h->num_sms = src->num_sms;
+    h->d_elem_u = src->d_elem_u;
+    h->d_elem_p = src->d_elem_p;
+    h->d_row_ptr = src->d_row_ptr;
+    h->d_uu_row_ptr = src->d_uu_row_ptr;
+    h->d_cp_row_ptr = src->d_cp_row_ptr;
+    h->d_wu = src->d_wu;
+    h->d_wp = src->d_wp;
+    h->d_elem_table = src->d_elem_table;
+    h->d_colour_elems = src->d_colour_elems;
+    h->d_tables = src->d_tables;
+    h->d_geo = src->d_geo;
+    h->d_geo_dd = src->d_geo_dd;
+    h->d_gbf_u = src->d_gbf_u;
+    h->d_gbf_p = src->d_gbf_p;
+    h->d_gw = src->d_gw;
+    h->d_bnd_elems = src->d_bnd_elems;
+    h->d_bnd_mask = src->d_bnd_mask;
+    h->d_u_inc_ptr = src->d_u_inc_ptr;
+    h->d_u_inc = src->d_u_inc;
+    h->d_p_inc_ptr = src->d_p_inc_ptr;
+    h->d_p_inc = src->d_p_inc;
+    h->high_precision = src->high_precision;
+    h->assembly_order = src->assembly_order;
+  }
+  auto fail = [&](int code) {
+    fe_destroy(h);
+    return code;
+  };
+  const size_t mat_bytes = sizeof(double) * h->hs.mat.size();
+  if (cudaMalloc(&h->d_mat, mat_bytes) != cudaSuccess ||
+      cudaMemcpy(h->d_mat, src->d_mat, mat_bytes, cudaMemcpyDeviceToDevice) != cudaSuccess ||
+      cudaMalloc(&h->d_status, sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(h->d_status, 0, sizeof(unsigned)) != cudaSuccess)
+    return fail(set_error(FE_ERR_CUDA, "clone: device allocation failed"));
+  if (src->has_surfp) {
+    const size_t bytes = sizeof(double) * 3 * (size_t)h->hs.nu;
+    if (cudaMalloc(&h->d_surfp, bytes) != cudaSuccess ||
+        cudaMemcpy(h->d_surfp, src->d_surfp, bytes, cudaMemcpyDeviceToDevice) != cudaSuccess)
+      return fail(set_error(FE_ERR_CUDA, "clone: device allocation failed"));
+    h->has_surfp = true;
+  }
+  *out = h;
   return FE_NO_ERROR;
 }
 
@@ -1204,7 +1292,7 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
   double* dc = values_coupling;
   double* dr = r;
   bool mapped_out = false;  // some output is host memory written in place: wait before returning
-  if (h->assembly_order == FE_ASSEMBLY_STAGED) {
+  if (h->assembly_order == FE_ASSEMBLY_STAGED && h->hs.gather_bytes > 0) {
     // the row gather writes each output row once, contiguously: page-locked
     // host outputs are written in place over the host link, with no device
     // copy of the result and no separate device-to-host copy

@@ -647,7 +647,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
           }
           const double accd = hd(acc);
           if constexpr (OUT == 1) {
-            SO->r[(size_t)elem_at(P, elems, grp * EG + el) * NROW + row] = accd;
+            SO->r[(size_t)elem_at(P, elems, grp * EG + el) * cmfe::rec_stride_r(NPE, NPP) + row] = accd;
           } else {
             const bool first = tab[ln * NR + ln] & 0x8000;
             if (first)
@@ -669,7 +669,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
           const H* rk = &s_dz[(el * 9 + n * 3) * NPE + b];
           const double kv = hd(rk[0] + rk[NPE] + rk[2 * NPE]);
           if constexpr (OUT == 1) {
-            SO->cp[(size_t)elem_at(P, elems, grp * EG + el) * NU3 + col] = kv;
+            SO->cp[(size_t)elem_at(P, elems, grp * EG + el) * cmfe::rec_stride_cp(NPE, NPP) + col] = kv;
             continue;
           }
           const int nb = nd[b], pq = nd[NPE];
@@ -748,7 +748,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
               const int q = q1 + 2 * q2 + 4 * q3, b = b1 + N1 * b2 + N2 * b3;
               const double kv = hd(acc);
               if constexpr (OUT == 1) {
-                SO->cp[((size_t)elem_at(P, elems, grp * EG + el) * 8 + q) * NU3 + n * NPE + b] = kv;
+                SO->cp[(size_t)elem_at(P, elems, grp * EG + el) * cmfe::rec_stride_cp(NPE, NPP) + q * NU3 + n * NPE + b] = kv;
                 continue;
               }
               const int lq = NPE + q, pq = nd[lq], nb = nd[b];
@@ -896,7 +896,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
               if (m == n && a < b) continue;
               const float v = acc[nt][h];
               if constexpr (OUT == 1) {
-                float* st = SO->uu + (size_t)elem_at(P, elems, grp * EG + el) * NU3 * NU3;
+                float* st = SO->uu + (size_t)elem_at(P, elems, grp * EG + el) * cmfe::rec_stride_uu(NPE);
                 st[(size_t)(m * NPE + a) * NU3 + n * NPE + b] = v;
                 if (!(m == n && a == b)) st[(size_t)(n * NPE + b) * NU3 + m * NPE + a] = v;
                 continue;

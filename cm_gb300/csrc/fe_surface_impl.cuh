@@ -130,7 +130,7 @@ __device__ __forceinline__ void surface_element(const cmfe::KParams& P, int e, c
         }
         const int a = S.node[f];
         if (mode == 2) {
-          SO->r[(size_t)e * nrow + c * NPE + a] += acc;
+          SO->r[(size_t)e * cmfe::rec_stride_r(NPE, nrow - 3 * NPE) + c * NPE + a] += acc;
         } else if (mode == 1) {
           P.elem_out[(size_t)(e - P.first_elem) * nrow + c * NPE + a] += acc;
         } else {
@@ -160,7 +160,7 @@ __device__ __forceinline__ void surface_element(const cmfe::KParams& P, int e, c
       if (mode == 2) {
         // the lower block entry and its mirror: distinct entries for distinct
         // (oh, ms, ns), so the lanes never touch the same word
-        float* st = SO->uu + (size_t)e * (3 * NPE) * (3 * NPE);
+        float* st = SO->uu + (size_t)e * cmfe::rec_stride_uu(NPE);
         const int R = mh * NPE + a, Cc = nh * NPE + b;
         st[(size_t)R * (3 * NPE) + Cc] += (float)acc;
         st[(size_t)Cc * (3 * NPE) + R] += (float)acc;

@@ -120,6 +120,18 @@ class FiniteElasticityEquationsSet:
         check(L.fe_mixed_layout(h, C.byref(nuu), C.byref(ncp), None, None))
         self.nnz_uu, self.nnz_coupling = nuu.value, ncp.value
 
+    def clone(self, materials=None):
+        """fe_clone: another equations set on the same mesh, sharing its
+        mesh-only device arrays; optionally with new materials."""
+        out = object.__new__(FiniteElasticityEquationsSet)
+        h = C.c_void_p()
+        check(_lib.load().fe_clone(self._h, C.byref(h)))
+        out.__dict__.update({k: v for k, v in self.__dict__.items() if k != "_h"})
+        out._h = h
+        if materials is not None:
+            out.set_materials(materials)
+        return out
+
     def close(self):
         if getattr(self, "_h", None):
             _lib.load().fe_destroy(self._h)

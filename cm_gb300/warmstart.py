@@ -334,13 +334,15 @@ def generate_solves(problem, params, increments, continuation=False):
     if continuation and n > 1:
         f = features(params)
         f = (f - f.mean(0)) / (f.std(0) + 1e-12)
-        left = set(range(1, n))
+        left = np.ones(n, dtype=bool)
+        left[0] = False
         order = [0]
-        while left:
-            last = f[order[-1]]
-            nxt = min(left, key=lambda j: float(((f[j] - last) ** 2).sum()))
+        for _ in range(n - 1):
+            d = ((f - f[order[-1]]) ** 2).sum(axis=1)
+            d[~left] = np.inf
+            nxt = int(np.argmin(d))
             order.append(nxt)
-            left.remove(nxt)
+            left[nxt] = False
     states = [None] * n
     iters = np.zeros(n, dtype=np.int64)
     prev = None

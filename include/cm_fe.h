@@ -158,6 +158,18 @@ int fe_mixed_layout(fe_handle h, int64_t* nnz_uu, int64_t* nnz_coupling, int32_t
  * every later residual and Jacobian evaluation. */
 int fe_set_surface_pressure(fe_handle h, const double* values);
 
+/* A second equations set on the same mesh (no counterpart in the reference,
+ * where each equations set builds its own structures): the clone shares the
+ * source's mesh-only device arrays -- pattern, rank tables, colouring,
+ * geometry cache, quadrature tables -- and the host pattern, and starts with
+ * copies of the source's materials, surface-pressure load and precision and
+ * assembly settings, which it then changes independently
+ * (fe_set_materials, fe_set_surface_pressure).  Shared arrays are freed with
+ * the last handle that uses them; handles may be destroyed in any order.
+ * Meant for many load / material variants of one geometry, e.g. the members
+ * of one fe_batch. */
+int fe_clone(fe_handle src, fe_handle* out);
+
 /* Replaces the material parameters given to fe_create (same layout: one set
  * of num_material_components values, or one per element when
  * materials_per_element was set), as an update of the reference's materials

@@ -194,8 +194,8 @@ def test_batch_member_limit(torch):
 
 def test_per_member_variant_is_the_single_set_path(torch):
     """Variant 5 launches the single-set kernels member by member: bit-identical
-    to one fe_jacobian_evaluate_mixed call per member, one launch per member
-    and colour (plus its surface faces), also from a captured graph."""
+    to one fe_jacobian_evaluate_mixed call per member (at least one launch per
+    member), also from a captured graph."""
     sets, xs, refs, batch = _setup(torch)
     vus, vcs, rs = batch.allocate("cuda")
     batch.set_config(5, 1, 1)
@@ -205,7 +205,7 @@ def test_per_member_variant_is_the_single_set_path(torch):
     batch.check(xs[0])
     for (a, b, c), u, v, w in zip(refs, vus, vcs, rs):
         assert torch.equal(a, u) and torch.equal(b, v) and torch.equal(c, w)
-    assert batch.launch_count() - l0 == sum(s.launch_count() - c for s, c in zip(sets, m0)) > len(sets)
+    assert batch.launch_count() - l0 == sum(s.launch_count() - c for s, c in zip(sets, m0)) >= len(sets)
     batch.capture(xs, vus, vcs, rs)
     for t in vus + vcs + rs:
         t.zero_()

@@ -380,3 +380,30 @@ def test_device_structure_calculation_large(torch):
         rp_h, col_h = structure_calculate(m)
         rp_d, col_d = structure_calculate(m, on_device=True)
         assert np.array_equal(rp_d, rp_h) and np.array_equal(col_d, col_h)
+
+
+def test_clone_shares_the_mesh_and_keeps_its_own_materials(torch):
+    """fe_clone: a clone with other materials (and a surface load) gives bit
+    for bit what a handle created from scratch for those materials gives,
+    and keeps working after the source handle is destroyed."""
+    m = meshes()["quad_node_guccione_fibres"]
+    x = torch.from_numpy(state(m)).cuda()
+    src = FiniteElasticityEquationsSet(m)
+    mats = np.array([1.3, 12.0, 2.5, 1.1])
+    cl = src.clone(mats)
+    sp = np.zeros((3, m.nu))
+    sp[2, m.node_ijk()[2] == 0] = 0.7
+    cl.set_surface_pressure(sp)
+    import copy
+    m2 = copy.copy(m)
+    m2.materials = mats
+    fresh = FiniteElasticityEquationsSet(m2)
+    fresh.set_surface_pressure(sp)
+    src.close()
+    for es in (cl, fresh):
+        es.r = torch.empty_like(x)
+    a = [t.clone() for t in cl.jacobian_evaluate_mixed(x, r=cl.r)] + [cl.r.clone()]
+    b = [t.clone() for t in fresh.jacobian_evaluate_mixed(x, r=fresh.r)] + [fresh.r.clone()]
+    cl.check_status(x)
+    assert all(torch.equal(u, v) for u, v in zip(a, b))
+    assert torch.equal(cl.jacobian_evaluate(x), fresh.jacobian_evaluate(x))
