@@ -444,6 +444,14 @@ def our_arm(args):
         out["plain_fp64"] = plain
     if dfloat:
         out["mixed_double_float"] = dfloat
+    if world == 1 and args.config == "cfg2" and args.extra:
+        # the batched configurations as extra keys: 256 box meshes, and 32
+        # variants of the full-size Guccione slab
+        torch.cuda.empty_cache()
+        out["batched_256_meshes"] = batch256_leg(dev, max(3, min(args.steps, 10)))
+        torch.cuda.empty_cache()
+        out["slab_variants_32"] = slab_variants_leg(dev, max(3, min(args.steps, 5)))
+        torch.cuda.empty_cache()
     if world == 1 and not args.no_cpu:
         rp1, col1 = es.csr_pattern(base=1)
         out["cpu_baseline"], vals_or, r_or = cpu_baseline(m, x, rp1, col1)
@@ -453,7 +461,7 @@ def our_arm(args):
         del es, r, xd
         torch.cuda.empty_cache()
         if args.config == "cfg5":
-            out["variants_batched"] = slab_variants_leg(dev, args.steps)
+            out["variants_batched"] = slab_variants_leg(dev, min(args.steps, 5))
             out["loadstep"] = slab_newton_leg(dev)
         else:
             out["loadstep"] = loadstep_leg(dev, n=args.loadstep_size, n_train=args.loadstep_train,
@@ -662,6 +670,52 @@ def loadstep_leg(dev, n=8, n_train=48, n_test=4, increments=8, modes=64, train_s
         "linear_solver": "GMRES + block-triangular preconditioner (multigrid V-cycle in a CUDA graph, "
                          "scaled pressure mass)",
     }
+
+
+def batch256_leg(dev, steps, n=256):
+    """The batched configuration as an extra key of the default line: 256
+    independent box meshes (seeded sizes, element types and materials) in one
+    batched call per assembly replayed from a CUDA graph with the autotuned
+    launch shape."""
+    import torch
+
+    from cm_gb300 import EquationsSetBatch, FiniteElasticityEquationsSet
+    from cm_gb300 import mesh as M
+    from cm_gb300.distributed import rank_batch_meshes
+    t0 = time.perf_counter()
+    meshes, stretches = rank_batch_meshes(n, 0)
+    sets = [FiniteElasticityEquationsSet(m) for m in meshes]
+    setup_s = time.perf_counter() - t0
+    xs = [torch.from_numpy(M.deformed_state(m, stretch=st, shear=0.0, noise=0.02, pressure=-1.0, seed=i)).to(dev)
+          for i, (m, st) in enumerate(zip(meshes, stretches))]
+    batch = EquationsSetBatch(sets)
+    vus, vcs, rs = batch.allocate(dev)
+    cfg = batch.autotune(xs, vus, vcs, rs, repeats=1)
+    batch.capture(xs, vus, vcs, rs)
+    for _ in range(3):
+        batch.replay(xs[0])
+    batch.check(xs[0])
+    stream = torch.cuda.current_stream(dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    l0 = batch.launch_count()
+    a.record(stream)
+    for _ in range(steps):
+        batch.replay(xs[0])
+    b.record(stream)
+    b.synchronize()
+    launches = (batch.launch_count() - l0) / steps
+    batch.check(xs[0])
+    t = a.elapsed_time(b) / 1e3 / steps
+    ne = sum(m.ne for m in meshes)
+    B = sum(algorithmic_bytes(m, s_, True) for m, s_ in zip(meshes, sets))
+    out = {"workload": "%d box meshes (edges U{4..24}, lengths U[0.5,2], trilinear/element-p or triquadratic/nodal-p "
+                       "50/50, MR c1,c2 log-U[0.5,10]), one batched call per assembly from a CUDA graph" % n,
+           "elements": ne, "value": ne / t, "unit": UNIT, "ms_per_step": 1e3 * t,
+           "kernel_launches_per_step": launches, "roofline_frac_hbm": B / t / 1e9 / peaks()["hbm_gbs"],
+           "algorithmic_bytes_per_step": B, "autotuned": cfg, "setup_s": setup_s}
+    batch.close()
+    return out
 
 
 def config2_loading_leg(dev, increments=10, stretch=1.2, shear=0.1):
@@ -951,6 +1005,8 @@ def main():
     ap.add_argument("--loadstep-increments", type=int, default=8, help="load increments of the plain method")
     ap.add_argument("--no-loadstep", dest="loadstep", action="store_false",
                     help="skip the Newton load-step comparison (plain FP64 vs mixed + learned warm start)")
+    ap.add_argument("--no-extra", dest="extra", action="store_false",
+                    help="skip the batched legs (256 box meshes, 32 slab variants) of the default configuration")
     ap.add_argument("--config2-loading", action="store_true",
                     help="only solve the 32^3 box's 10-increment loading (plain FP64 vs mixed) and print it")
     ap.add_argument("--config4-study", action="store_true",

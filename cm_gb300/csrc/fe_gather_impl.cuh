@@ -40,47 +40,6 @@ __device__ __forceinline__ T rec_load(const T* p) {
     return *p;
 }
 
-// Drops the records of element e from L2 without writing them back (every
-// row node of the element has been gathered, so no one reads them again in
-// this assembly, and the next assembly rewrites them): the records are lines
-// of 128 bytes each (line-aligned strides), discarded by one warp.
-template <int NPE, int NPP>
-__device__ __forceinline__ void discard_records(const cmfe::StageOut& S, int e, int lane) {
-  constexpr int LU = cmfe::rec_stride_uu(NPE) * 4 / 128, LC = cmfe::rec_stride_cp(NPE, NPP) * 8 / 128,
-                LR = cmfe::rec_stride_r(NPE, NPP) * 8 / 128;
-  const char* u = reinterpret_cast<const char*>(S.uu + (size_t)e * cmfe::rec_stride_uu(NPE));
-  const char* c = reinterpret_cast<const char*>(S.cp + (size_t)e * cmfe::rec_stride_cp(NPE, NPP));
-  const char* r = reinterpret_cast<const char*>(S.r + (size_t)e * cmfe::rec_stride_r(NPE, NPP));
-  for (int i = lane; i < LU + LC + LR; i += 32) {
-    const char* p = i < LU ? u + 128 * i : (i < LU + LC ? c + 128 * (i - LU) : r + 128 * (i - LU - LC));
-    asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
-  }
-}
-
-// Counts one more gathered row node for every element around a node (the
-// incidences k0 .. k1 - 1 of the packed list, element = packed >> shift) and
-// drops the records of those elements whose row nodes are all gathered.
-template <int NPE, int NPP>
-__device__ __forceinline__ void release_elements(const cmfe::StageOut& S, int* elem_done, const int32_t* inc, int k0,
-                                                 int k1, int shift, int lane) {
-  constexpr int NR = NPE + NPP;
-  for (int kb = k0; kb < k1; kb += 32) {
-    const int k = kb + lane;
-    bool last = false;
-    int e = 0;
-    if (k < k1) {
-      e = inc[k] >> shift;
-      last = atomicAdd(elem_done + e, 1) + 1 == NR;
-    }
-    unsigned m = __ballot_sync(0xffffffffu, last);
-    while (m) {
-      const int src = __ffs(m) - 1;
-      m &= m - 1;
-      discard_records<NPE, NPP>(S, __shfl_sync(0xffffffffu, e, src), lane);
-    }
-  }
-}
-
 // The three displacement rows of u node a, by one warp; `mine` is the warp's
 // shared scratch (36 wu bytes rounded up to 16, then 24 wc bytes).
 template <int NPE, int NPP, bool CG>

@@ -107,9 +107,9 @@ struct KParams {
 #endif
 
 // Strides of the per-element records of the staged assembly, in elements of
-// each record's type, rounded up to whole 128-byte lines so that the fused
-// kernel can drop a consumed record from L2 line by line without touching a
-// neighbour's (npe u nodes and npp pressure parameters per element).
+// each record's type, rounded up to whole 128-byte lines, so that no L2 line
+// holds parts of two elements' records (npe u nodes and npp pressure
+// parameters per element).
 CMFE_HD constexpr int rec_stride_uu(int npe) { return (9 * npe * npe + 31) / 32 * 32; }          // floats
 CMFE_HD constexpr int rec_stride_cp(int npe, int npp) { return (npp * 3 * npe + 15) / 16 * 16; }  // doubles
 CMFE_HD constexpr int rec_stride_r(int npe, int npp) { return (3 * npe + npp + 15) / 16 * 16; }   // doubles
@@ -136,7 +136,6 @@ struct FusedArgs {
   const int32_t* p_inc;
   int* work;
   int* node_done;
-  int* elem_done;  // per element: how many of its row nodes are gathered (zero before the launch)
   const uint8_t* bmask;
   int gwarps;  // warps that gather (set by the launcher)
   int gbytes;  // scratch bytes per gathering warp (set by the launcher)

@@ -635,7 +635,7 @@ int mixed_staged(fe_handle h, const double* dx, float* du, double* dc, double* d
   const int nb = s.bnd_ptr.empty() ? 0 : s.bnd_ptr[s.ncolours];
   if (cmfe::fused_fits(s)) {
     // one launch: element records and row gathers together
-    const size_t counters = 1 + (size_t)s.nu + (size_t)s.npn + (size_t)s.ne;
+    const size_t counters = 1 + (size_t)s.nu + (size_t)s.npn;
     if ((rc = ensure((void**)&h->d_fuse, sizeof(int) * counters))) return rc;
     CUDA_TRY(cudaMemsetAsync(h->d_fuse, 0, sizeof(int) * counters, st));
     cmfe::FusedArgs fa;
@@ -646,7 +646,6 @@ int mixed_staged(fe_handle h, const double* dx, float* du, double* dc, double* d
     fa.p_inc = h->d_p_inc;
     fa.work = h->d_fuse;
     fa.node_done = h->d_fuse + 1;
-    fa.elem_done = h->d_fuse + 1 + s.nu + s.npn;
     fa.bmask = h->has_surfp && nb > 0 ? h->d_bnd_mask : nullptr;
     const int e = cmfe::launch_mixed_fused(s, kp, so, fa, h->num_sms, st, double_float);
     if (e != 0)

@@ -43,8 +43,6 @@ __global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB) fe_mixed_staged_ker
 // another.  Publication follows the release/acquire pattern: every thread
 // fences its record stores before the counting, and a completing count is
 // followed by a fence before the records are read (through L2, not L1).
-// Once all row nodes of an element are gathered, its records are dropped
-// from L2 unwritten (discard.global.L2): they never reach DRAM.
 template <int N1, int PM, int SPLIT, class H>
 __global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB)
     fe_mixed_fused_kernel(KParams P, cmfe::StageOut so, cmfe::FusedArgs F) {
@@ -94,14 +92,10 @@ __global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB)
       unsigned char* mine = scratch + (size_t)warp * F.gbytes;
       for (int j = warp; j < nready; j += F.gwarps) {
         const int id = ready[j];
-        if (id < P.nu) {
+        if (id < P.nu)
           gather_unode<NPE, NPP, true>(P, so, F.u_inc_ptr, F.u_inc, id, mine, lane);
-          release_elements<NPE, NPP>(so, F.elem_done, F.u_inc, F.u_inc_ptr[id], F.u_inc_ptr[id + 1], 5, lane);
-        } else {
+        else
           gather_pnode<NPE, NPP, true>(P, so, F.p_inc_ptr, F.p_inc, id - P.nu, mine, lane);
-          release_elements<NPE, NPP>(so, F.elem_done, F.p_inc, F.p_inc_ptr[id - P.nu], F.p_inc_ptr[id - P.nu + 1], 3,
-                                     lane);
-        }
       }
     }
     __syncthreads();  // the next group reuses the scratch and the ready list
