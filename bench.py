@@ -679,12 +679,12 @@ def batch256_leg(dev, steps, n=256):
     launch shape."""
     import torch
 
-    from cm_gb300 import EquationsSetBatch, FiniteElasticityEquationsSet
+    from cm_gb300 import EquationsSetBatch, create_equations_sets
     from cm_gb300 import mesh as M
     from cm_gb300.distributed import rank_batch_meshes
     t0 = time.perf_counter()
     meshes, stretches = rank_batch_meshes(n, 0)
-    sets = [FiniteElasticityEquationsSet(m) for m in meshes]
+    sets = create_equations_sets(meshes)
     setup_s = time.perf_counter() - t0
     xs = [torch.from_numpy(M.deformed_state(m, stretch=st, shear=0.0, noise=0.02, pressure=-1.0, seed=i)).to(dev)
           for i, (m, st) in enumerate(zip(meshes, stretches))]
@@ -878,7 +878,7 @@ def batch_arm(args):
     import numpy as np
     import torch
 
-    from cm_gb300 import EquationsSetBatch, FiniteElasticityEquationsSet
+    from cm_gb300 import EquationsSetBatch, create_equations_sets
     from cm_gb300 import mesh as M
     from cm_gb300.distributed import max_over_ranks, rank_batch_meshes
     rank = int(os.environ.get("RANK", "0"))
@@ -892,7 +892,7 @@ def batch_arm(args):
     dev = torch.device("cuda", local)
     t0 = time.perf_counter()
     meshes, stretches = rank_batch_meshes(args.batch_meshes, rank)
-    sets = [FiniteElasticityEquationsSet(m) for m in meshes]
+    sets = create_equations_sets(meshes)
     setup_s = time.perf_counter() - t0
     xs_h = [M.deformed_state(m, stretch=s, shear=0.0, noise=0.02, pressure=-1.0, seed=i)
             for i, (m, s) in enumerate(zip(meshes, stretches))]

@@ -61,9 +61,8 @@ struct HostSetup {
   // node (sorted by element number, packed e * 32 + local node) and around
   // every pressure row node (e * 8 + local pressure node).
   std::vector<int32_t> u_inc_ptr, u_inc, p_inc_ptr, p_inc;
-  // shared memory one gather warp needs (its incidence record and inverse
-  // rank maps); 0 when some row node has more than 32 elements around it, in
-  // which case the mixed assembly runs in colour order
+  // shared memory one gather warp needs: the larger of a u node's three rows
+  // (3 x 3 wu FP32, then 3 x its pressure columns FP64) and a pressure row (FP64)
   int gather_bytes = 0;
 };
 

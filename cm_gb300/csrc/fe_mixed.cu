@@ -76,6 +76,7 @@ __global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB)
     if (tid == 0) s_nready = 0;
     __syncthreads();
     for (int i = tid; i < nvalid * NR; i += C::THREADS) {
+      __threadfence();  // cumulative release, after the barrier, for the stores of the whole CTA
       const int el = i / NR, r = i % NR;
       const int node = s_node[el * (NR + 1) + r];
       const bool un = r < NPE;

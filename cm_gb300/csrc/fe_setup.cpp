@@ -301,24 +301,21 @@ int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg) {
   s.nnz_uu = nuu;
   s.nnz_cp = ncp;
   {
-    // scratch of one gathering warp: the incidence record (two arrays of 32
-    // ints) and an inverse rank map of one byte per incidence and column; 0
-    // (no staged assembly) when a row node has more than 32 elements around it
+    // scratch of one gathering warp: the larger of a u node's three rows
+    // (3 x 3 wu FP32, padded to 16 bytes, then 3 x its pressure columns FP64)
+    // and a pressure row (FP64)
     int64_t need = 0;
-    bool fits = true;
     for (int n = 0; n < s.nu; ++n) {
-      const int64_t nk = (int64_t)surr_u[n].size();
       const int64_t wc = s.cp_row_ptr[(size_t)n + 1] - s.cp_row_ptr[(size_t)n];
-      fits = fits && nk <= 32;
-      need = std::max<int64_t>(need, 256 + nk * (s.wu[n] + wc));
+      need = std::max<int64_t>(need, ((36 * (int64_t)s.wu[n] + 15) & ~(int64_t)15) + 3 * wc * 8);
     }
     for (int q = 0; q < s.npn; ++q) {
-      const int64_t nk = (int64_t)surr_p[q].size();
-      fits = fits && nk <= 32;
-      need = std::max<int64_t>(need, 256 + nk * s.wp[q]);
+      const size_t row = (size_t)3 * s.nu + q;
+      need = std::max<int64_t>(need, (int64_t)(s.cp_row_ptr[row + 1] - s.cp_row_ptr[row]) * 8);
     }
-    s.gather_bytes = fits ? (int)std::min<int64_t>((need + 15) & ~(int64_t)15, 1 << 30) : 0;
+    s.gather_bytes = (int)std::min<int64_t>((need + 15) & ~(int64_t)15, 1 << 30);
   }
+
 
   s.col.allocate(nnz);
   parallel_for((int)s.ndofs, [&](int r) {

@@ -294,6 +294,23 @@ class FiniteElasticityEquationsSet:
         return out
 
 
+def create_equations_sets(meshes, threads=None):
+    """One FiniteElasticityEquationsSet per mesh, created concurrently: each
+    fe_create builds its mesh's set-up (pattern, rank tables, colouring,
+    geometry cache) on the host and uploads it, and the C call releases the
+    interpreter, so many small meshes set up in parallel on the host cores.
+    Returns the sets in the order of `meshes`."""
+    import concurrent.futures as cf
+    import os
+    meshes = list(meshes)
+    if threads is None:
+        threads = min(len(meshes), os.cpu_count() or 1)
+    if threads <= 1:
+        return [FiniteElasticityEquationsSet(m) for m in meshes]
+    with cf.ThreadPoolExecutor(threads) as ex:
+        return list(ex.map(FiniteElasticityEquationsSet, meshes))
+
+
 class EquationsSetBatch:
     """Many independent equations sets assembled in one persistent launch
     (fe_batch_* of include/cm_fe.h).  Buffers are CUDA tensors."""

@@ -237,3 +237,20 @@ def test_grid_barrier_gives_up_and_reports(torch):
     _close(torch, refs, vus, vcs, rs)
     with pytest.raises(FEError):
         b.set_barrier_limits(0, 1)  # an unreachable barrier needs a small poll limit
+
+
+def test_concurrent_creation_matches_serial(torch):
+    """create_equations_sets builds the members' set-ups on several host
+    threads: the same patterns and the same assembled values as handles
+    created one after another."""
+    from cm_gb300 import FiniteElasticityEquationsSet, create_equations_sets
+    ms = members()
+    par = create_equations_sets(ms, threads=8)
+    for m, es in zip(ms, par):
+        ref = FiniteElasticityEquationsSet(m)
+        a, b = ref.csr_pattern(), es.csr_pattern()
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+        x = torch.from_numpy(M.deformed_state(m, stretch=1.04, shear=0.02, noise=0.02, seed=3)).cuda()
+        ua, ca = ref.jacobian_evaluate_mixed(x)
+        ub, cb = es.jacobian_evaluate_mixed(x)
+        assert torch.equal(ua, ub) and torch.equal(ca, cb)
