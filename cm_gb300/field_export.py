@@ -25,43 +25,75 @@ def _basis_label(nxi):
     return "*".join([lab] * 3)
 
 
-def _node_fields(mesh: Mesh, x):
+def _node_components(mesh: Mesh):
+    """Node-based components carried by every node, in field order: the
+    geometric field's x, y, z, then the dependent field's three position
+    components and, on the pressure (corner) nodes of a nodal pressure, its
+    fourth (pressure) component."""
+    has_p = np.zeros(mesh.nu, dtype=bool)
+    if mesh.p_mode == 1:
+        has_p[mesh.pressure_node_u()] = True
+    return [7 if has_p[n] else 6 for n in range(mesh.nu)]
+
+
+def _group_nodes(ncomp):
+    """Node order of the reference's nodal information set sort
+    (FIELD_IO_NODAL_INFO_SET_SORT, field_IO_routines.f90:4452-4520): each
+    node's later namesakes (same component set) are swapped in right behind
+    it; returns the order and whether each position repeats the previous
+    header."""
+    n = len(ncomp)
+    order = list(range(n))
+    repeat = [False] * n
+    i = 0
+    while i < n - 1:
+        key = ncomp[order[i]]
+        for j in range(i + 1, n):
+            if ncomp[order[j]] == key:
+                order[j], order[i + 1] = order[i + 1], order[j]
+                repeat[j] = False
+                repeat[i + 1] = True
+                i += 1
+        i += 1
+    return order, repeat
+
+
+def write_exnode(path, mesh: Mesh, x, group="Region", geometry="Geometry", dependent="Dependent"):
+    """Nodal values of the geometric field and of the dependent field
+    (deformed position and, for nodal pressure, the hydrostatic pressure on
+    the pressure nodes) in the layout the reference's FieldExport.c writes
+    when FIELD_IO_NODES_EXPORT exports these two fields: one header per run
+    of nodes with the same component set (the dependent variable lists four
+    components on every node; nodes without pressure carry six values, as in
+    the reference's output), then one value per line in %.16E."""
     nu = mesh.nu
     z = np.asarray(x[:3 * nu], dtype=np.float64).reshape(3, nu)
-    fields = [("Geometry", "coordinate, rectangular cartesian", ("x", "y", "z"), mesh.X),
-              ("DeformedGeometry", "field, rectangular cartesian", ("x", "y", "z"), z)]
-    return fields
-
-
-def write_exnode(path, mesh: Mesh, x, group="FiniteElasticity"):
-    """Nodal values of the geometry and the deformed geometry (one value per
-    node and component), plus the nodal pressure on the pressure nodes."""
-    fields = _node_fields(mesh, x)
-    nu = mesh.nu
-    lines = [" Group name: %s" % group, " #Fields=%d" % len(fields)]
-    for i, (name, kind, comps, _) in enumerate(fields, start=1):
-        lines.append(" %d) %s, %s, #Components=%d" % (i, name, kind, len(comps)))
-        for j, c in enumerate(comps):
-            lines.append("   %s.  Value index=%d, #Derivatives=0" % (c, 1 + j))
-    for n in range(nu):
-        lines.append(" Node:            %d" % (n + 1))
-        for _, _, _, vals in fields:
-            lines.append("   " + "  ".join("%.17e" % vals[c, n] for c in range(3)))
+    p = np.zeros(nu)
     if mesh.p_mode == 1:
-        p = np.asarray(x[3 * nu:], dtype=np.float64)
-        pnode = mesh.pressure_node_u()
-        lines.append(" #Fields=1")
-        lines.append(" 1) HydrostaticPressure, field, rectangular cartesian, #Components=1")
-        lines.append("   1.  Value index=1, #Derivatives=0")
-        order = np.argsort(pnode)
-        for q in order:
-            lines.append(" Node:            %d" % (pnode[q] + 1))
-            lines.append("   %.17e" % p[q])
+        p[mesh.pressure_node_u()] = np.asarray(x[3 * nu:], dtype=np.float64)
+    ncomp = _node_components(mesh)
+    order, repeat = _group_nodes(ncomp)
+    header = [" #Fields=2",
+              " 1) %s, coordinate, rectangular cartesian, #Components=3" % geometry,
+              "   x.  Value index= 1, #Derivatives= 0",
+              "   y.  Value index= 2, #Derivatives= 0",
+              "   z.  Value index= 3, #Derivatives= 0",
+              " 2) %s, field,  rectangular cartesian, #Components=4" % dependent]
+    header += ["   %d.  Value index= %d, #Derivatives= 0" % (c, 3 + c) for c in (1, 2, 3, 4)]
+    lines = [" Group name: %s" % group]
+    for pos, n in enumerate(order):
+        if not repeat[pos]:
+            lines += header
+        lines.append(" Node:            %d" % (n + 1))
+        vals = [mesh.X[0, n], mesh.X[1, n], mesh.X[2, n], z[0, n], z[1, n], z[2, n]]
+        if ncomp[n] == 7:
+            vals.append(p[n])
+        lines += ["  %.16E" % v for v in vals]
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
 
 
-def write_exelem(path, mesh: Mesh, x=None, group="FiniteElasticity"):
+def write_exelem(path, mesh: Mesh, x=None, group="Region"):
     """Element topology with the node-based interpolation of the two
     geometric fields; element-constant pressure (when x is given and the
     pressure is element based) as a constant, grid-based field."""
@@ -100,7 +132,7 @@ def write_exelem(path, mesh: Mesh, x=None, group="FiniteElasticity"):
         f.write("\n".join(lines) + "\n")
 
 
-def export(prefix, mesh: Mesh, x, group="FiniteElasticity"):
+def export(prefix, mesh: Mesh, x, group="Region"):
     """Writes prefix.exnode and prefix.exelem for the state x (host array or
     tensor in the library's dof order)."""
     if hasattr(x, "detach"):
@@ -111,22 +143,19 @@ def export(prefix, mesh: Mesh, x, group="FiniteElasticity"):
 
 
 def read_exnode_values(path):
-    """Parses the node blocks of a file written by write_exnode: returns
-    {field group index: {node number: values}} for checking round trips."""
-    out, block = {}, -1
-    node = None
+    """Parses a file written by write_exnode: {node number: values} (six or
+    seven per node) for checking round trips."""
+    out, node = {}, None
     with open(path) as f:
         for ln in f:
             s = ln.strip()
-            if s.startswith("#Fields="):
-                block += 1
-                out[block] = {}
-                node = None
-            elif s.startswith("Node:"):
+            if s.startswith("Node:"):
                 node = int(s.split()[1])
-                out[block][node] = []
+                out[node] = []
+            elif s.startswith("#Fields=") or s.startswith("Group"):
+                node = None
             elif node is not None and s and s[0] in "-0123456789":
-                out[block][node] += [float(v) for v in s.split()]
+                out[node] += [float(v) for v in s.split()]
     return out
 
 

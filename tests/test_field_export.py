@@ -1,10 +1,34 @@
-"""exnode/exelem export of a state (the reference's field export layout):
-values and element topology read back exactly."""
+"""exnode/exelem export of a state.
+
+The exnode file is compared byte for byte with the reference's own writer,
+src/FieldExport.c, compiled unchanged from the reference tree
+(oracle/build.py build_ref) and driven the way the reference's
+FIELD_IO_NODES_EXPORT drives it (oracle/fieldexport_ref.py); the test is
+skipped where the reference tree is absent.  Values and element topology
+also read back exactly.
+"""
+import os
+
 import numpy as np
 import pytest
 
 from cm_gb300 import field_export as F
 from cm_gb300 import mesh as M
+
+
+@pytest.mark.parametrize("nxi,pmode", [(3, "node"), (2, "element"), (2, "node")])
+def test_exnode_matches_the_reference_writer(tmp_path, nxi, pmode):
+    import build as ob  # oracle/build.py
+    if ob.build_ref() is None:
+        pytest.skip("the reference tree is not on this machine")
+    import fieldexport_ref as R  # oracle/fieldexport_ref.py
+    m = M.regular_box(2, 3, 2, nxi_u=nxi, pressure=pmode, perturb=0.1, seed=4)
+    x = M.deformed_state(m, stretch=1.1, shear=0.05, noise=0.02, pressure=-1.3, seed=5)
+    ours, ref = str(tmp_path / "ours.exnode"), str(tmp_path / "ref.exnode")
+    F.write_exnode(ours, m, x, group="Region")
+    R.write_exnode(ref, m, x, group="Region")
+    assert os.path.getsize(ref) > 0
+    assert open(ours).read() == open(ref).read()
 
 
 @pytest.mark.parametrize("nxi,pmode", [(3, "node"), (2, "element")])
@@ -13,14 +37,15 @@ def test_export_round_trip(tmp_path, nxi, pmode):
     x = M.deformed_state(m, stretch=1.1, shear=0.05, noise=0.02, pressure=-1.3, seed=5)
     node_file, elem_file = F.export(str(tmp_path / "state"), m, x)
     vals = F.read_exnode_values(node_file)
+    pnode = set(m.pressure_node_u().tolist()) if pmode == "node" else set()
     for n in range(m.nu):
-        v = vals[0][n + 1]
+        v = vals[n + 1]
         assert v[:3] == list(m.X[:, n])
-        assert v[3:] == [x[c * m.nu + n] for c in range(3)]
+        assert v[3:6] == [x[c * m.nu + n] for c in range(3)]
+        assert len(v) == (7 if n in pnode else 6)
     if pmode == "node":
-        pnode = m.pressure_node_u()
-        for q in range(m.np):
-            assert vals[1][pnode[q] + 1] == [x[3 * m.nu + q]]
+        for q, n in enumerate(m.pressure_node_u()):
+            assert vals[n + 1][6] == x[3 * m.nu + q]
     elems = F.read_exelem_nodes(elem_file)
     assert len(elems) == m.ne
     for e in range(m.ne):
