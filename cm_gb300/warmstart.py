@@ -290,6 +290,14 @@ class ParametricProblem:
         torch.cuda.synchronize(self.device) if self.device.type == "cuda" else None
         return x, reps, time.perf_counter() - t0
 
+    def newton_from_state(self, p, state):
+        """Newton at the full load of parameters p from the free-dof state
+        `state`, without a fallback: (x, report)."""
+        self.set_parameters(p)
+        x = self.solver.apply_increment(self.x_init.clone(), 1, 1)
+        x[self.free] = self.x_init[self.free] + state
+        return self.solver.newton(x)
+
     def solve_from_state(self, p, state, fallback_increments):
         """One full-load increment from a predicted state; the reference
         method if that does not converge.  Returns (x, reports, seconds,
@@ -319,16 +327,24 @@ def sample_parameters(n, seed, stretch=(1.0, 1.3), shear=(0.0, 0.2), c_range=(0.
     return np.stack([lam, gam, c1, c2], axis=1)
 
 
-def generate_solves(problem, params, increments, continuation=False):
+def _interpolate_parameters(a, b, t):
+    """(stretch, shear, c1, c2) between a and b: stretch and shear linearly,
+    the moduli geometrically."""
+    return np.array([a[0] + t * (b[0] - a[0]), a[1] + t * (b[1] - a[1]),
+                     a[2] * (b[2] / a[2]) ** t, a[3] * (b[3] / a[3]) ** t])
+
+
+def generate_solves(problem, params, increments, continuation=False, steps=1):
     """Converged free-dof states for every parameter row.
 
     Without continuation every row is solved by the plain method (reference
     guess, load increments).  With continuation the rows are visited along a
     greedy nearest-neighbour path in feature space and each solve starts from
-    the previous converged state in one increment (the plain method where
-    that fails); the converged states are the same (||r||_2 <= atol), only
-    cheaper to reach.  Returns (states in the order of params, Newton
-    iterations per row)."""
+    the previous converged state, walking to the new parameters in `steps`
+    full-load Newton solves at parameters interpolated between the two (the
+    plain method where one of them does not converge); the converged states
+    are the same (||r||_2 <= atol), only cheaper to reach.  Returns (states in
+    the order of params, Newton iterations per row)."""
     n = len(params)
     order = list(range(n))
     if continuation and n > 1:
@@ -346,9 +362,22 @@ def generate_solves(problem, params, increments, continuation=False):
     states = [None] * n
     iters = np.zeros(n, dtype=np.int64)
     prev = None
+    prev_p = None
     for i in order:
         p = params[i]
-        if prev is not None:
+        if prev is not None and steps > 1 and hasattr(problem, "newton_from_state"):
+            reps, st, ok = [], prev, True
+            for k in range(1, steps + 1):
+                x, rep = problem.newton_from_state(_interpolate_parameters(prev_p, p, k / steps), st)
+                reps.append(rep)
+                if not rep.converged:
+                    ok = False
+                    break
+                st = problem.state(x)
+            if not ok:
+                x, more, _ = problem.solve_reference(p, increments)
+                reps += more
+        elif prev is not None:
             x, reps, _, _ = problem.solve_from_state(p, prev, increments)
         else:
             x, reps, _ = problem.solve_reference(p, increments)
@@ -357,6 +386,7 @@ def generate_solves(problem, params, increments, continuation=False):
         states[i] = problem.state(x)
         iters[i] = sum(r.iterations for r in reps)
         prev = states[i] if continuation else None
+        prev_p = p
     return torch.stack(states), iters
 
 
