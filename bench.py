@@ -404,6 +404,31 @@ def our_arm(args):
     te = max_over_ranks(te, dist, dev)
     e2e = {"value": world * m.ne * k_e2e / te, "unit": UNIT, "h2d_bytes_per_step": 8 * es.ndofs,
            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * te / k_e2e}
+    if mixed:
+        # the other host-output modes of the same call, for comparison
+        e2e["host_output"] = "streamed"
+        others = {}
+        for mode in ("in_place", "after"):
+            es.set_host_output(mode)
+            e2e_step()
+            t0 = time.perf_counter()
+            for _ in range(k_e2e):
+                e2e_step()
+            others[mode] = {"ms_per_step": 1e3 * (time.perf_counter() - t0) / k_e2e}
+        es.set_host_output("streamed")
+        e2e["other_host_outputs"] = others
+        # the host link for comparison: plain device-to-host copies of the same
+        # result arrays into the same pinned buffers
+        srcs = [(vu, torch.from_numpy(vuh)), (vc, torch.from_numpy(vch)), (r, torch.from_numpy(rh))]
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(3):
+            for a_, b_ in srcs:
+                b_.copy_(a_, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        tl = (time.perf_counter() - t0) / 3
+        e2e["host_link"] = {"d2h_copy_ms": 1e3 * tl, "d2h_copy_gbs": d2h / tl / 1e9,
+                            "note": "plain pinned device-to-host copies of the same result bytes"}
 
     if rank != 0:
         if dist:
@@ -433,7 +458,7 @@ def our_arm(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "traffic": traffic, "peak_source": pk["source"],
-                     "kernel": "fe_mixed_kernel" if mixed else "fe_element_kernel",
+                     "kernel": "fe_mixed_fused_kernel" if mixed else "fe_element_kernel",
                      "launches_per_step": launches / args.steps,
                      "algorithmic_bytes_per_launch": B * args.steps / max(launches, 1),
                      "traffic_unit": "DRAM bytes per launch (ncu, profiles/traffic.json)",
@@ -718,7 +743,7 @@ def batch256_leg(dev, steps, n=256):
     return out
 
 
-def config2_loading_leg(dev, increments=10, stretch=1.2, shear=0.1):
+def config2_loading_leg(dev, increments=10, stretch=1.2, shear=0.1, arms_wanted=None):
     """The single-large-mesh configuration's loading: the 32^3 triquadratic
     box (859,812 dofs) clamped at x = 0 and moved to stretch 1.2 / shear 0.1
     on x = 1 in 10 load increments (the reference's fixed-incremented rule),
@@ -738,13 +763,22 @@ def config2_loading_leg(dev, increments=10, stretch=1.2, shear=0.1):
     arms = {"plain_fp64": N.NewtonOptions(linear="mg"),
             "mixed": N.NewtonOptions(linear="mg", precision="mixed"),
             "mixed_ew": N.NewtonOptions(linear="mg", precision="mixed", forcing="ew")}
+    if arms_wanted:
+        arms = {k: v for k, v in arms.items() if k in arms_wanted}
     out, xs = {}, {}
     for name, opt in arms.items():
         solver = N.LoadStepSolver(es, bc, opt, device=dev)
         x0 = torch.from_numpy(N.initial_state(m)).to(dev)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        x, reps = solver.solve(x0, increments)
+
+        def progress(i, rep, name=name, t0=t0):
+            print("config2 %s increment %d: %s, %d Newton, %d Krylov, assembly %.2f s, linear %.2f s "
+                  "(multigrid set-up %.2f s), %.1f s so far"
+                  % (name, i, "converged" if rep.converged else "not converged", rep.iterations,
+                     sum(rep.linear_iterations), rep.assembly_seconds, rep.linear_seconds,
+                     rep.preconditioner_seconds, time.perf_counter() - t0), file=sys.stderr, flush=True)
+        x, reps = solver.solve(x0, increments, progress=progress)
         torch.cuda.synchronize(dev)
         t = time.perf_counter() - t0
         xs[name] = x
@@ -755,15 +789,19 @@ def config2_loading_leg(dev, increments=10, stretch=1.2, shear=0.1):
                      "converged_1e-10": bool(all(r.converged for r in reps) and len(reps) == increments),
                      "final_residual": float(reps[-1].residual_norms[-1]),
                      "assembly_s": float(sum(r.assembly_seconds for r in reps)),
-                     "linear_s": float(sum(r.linear_seconds for r in reps))}
+                     "linear_s": float(sum(r.linear_seconds for r in reps)),
+                     "multigrid_setup_s": float(sum(r.preconditioner_seconds for r in reps))}
         del solver
         torch.cuda.empty_cache()
-    ref = xs["plain_fp64"]
-    for name in ("mixed", "mixed_ew"):
-        out[name]["max_solution_difference"] = float((xs[name] - ref).abs().max())
+    if "plain_fp64" in xs:
+        ref = xs["plain_fp64"]
+        for name in ("mixed", "mixed_ew"):
+            if name in xs:
+                out[name]["max_solution_difference"] = float((xs[name] - ref).abs().max())
     out["workload"] = ("32^3 triquadratic-u/trilinear-p box (%d dofs), MR c1=2 c2=6, x=0 clamped, x=1 moved to "
                        "stretch %.2f + shear %.2f in %d increments" % (es.ndofs, stretch, shear, increments))
-    out["speedup_mixed_ew"] = out["plain_fp64"]["solve_ms"] / out["mixed_ew"]["solve_ms"]
+    if "plain_fp64" in out and "mixed_ew" in out:
+        out["speedup_mixed_ew"] = out["plain_fp64"]["solve_ms"] / out["mixed_ew"]["solve_ms"]
     return out
 
 
@@ -1009,6 +1047,8 @@ def main():
                     help="skip the Newton load-step comparison (plain FP64 vs mixed + learned warm start)")
     ap.add_argument("--no-extra", dest="extra", action="store_false",
                     help="skip the batched legs (256 box meshes, 32 slab variants) of the default configuration")
+    ap.add_argument("--config2-arms", default="",
+                    help="comma-separated arms of --config2-loading (plain_fp64, mixed, mixed_ew; default all)")
     ap.add_argument("--config2-loading", action="store_true",
                     help="only solve the 32^3 box's 10-increment loading (plain FP64 vs mixed) and print it")
     ap.add_argument("--config4-study", action="store_true",
@@ -1027,7 +1067,8 @@ def main():
     if args.config2_loading:
         import torch
         torch.cuda.set_device(0)
-        print(json.dumps({"config2_loading": config2_loading_leg(torch.device("cuda", 0))}))
+        arms = args.config2_arms.split(",") if args.config2_arms else None
+        print(json.dumps({"config2_loading": config2_loading_leg(torch.device("cuda", 0), arms_wanted=arms)}))
         return
     if args.impl == "reference":
         reference_arm(args)

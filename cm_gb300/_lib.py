@@ -28,6 +28,9 @@ FE_HIGH_PRECISION_FP64 = 0
 FE_HIGH_PRECISION_DOUBLE_FLOAT = 1
 FE_ASSEMBLY_STAGED = 0
 FE_ASSEMBLY_COLOURED = 1
+FE_HOST_OUTPUT_STREAMED = 0
+FE_HOST_OUTPUT_IN_PLACE = 1
+FE_HOST_OUTPUT_AFTER = 2
 FE_PRESSURE_ELEMENT_BASED = 0
 FE_PRESSURE_NODE_BASED = 1
 FE_NOALLOC_MAX_DOFS = 1048576
@@ -84,6 +87,7 @@ SIGNATURES = {
     "fe_element_jacobians": [_vp, _vp, _i32, _i32, _vp, _vp],
     "fe_set_high_precision": [_vp, _i32],
     "fe_set_assembly_order": [_vp, _i32],
+    "fe_set_host_output": [_vp, _i32, _i32],
     "fe_clone": [_vp, C.POINTER(_vp)],
     "fe_set_surface_pressure": [_vp, _vp],
     "fe_set_materials": [_vp, _vp],

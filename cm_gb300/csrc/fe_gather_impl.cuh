@@ -13,6 +13,11 @@
 // (distributed_matrix_vector.f90:8853-8927), organised by rows instead of by
 // elements: every matrix sector is written once, in full, and never read.
 //
+// The incidences of a row node are read 32 at a time, lane i loading
+// incidence i and its element's rank-table row, and handed to the warp by
+// shuffles: the loads of one incidence (its ranks and record values) then
+// depend on no other load.
+//
 // Row layout (the mixed split of the handle): a displacement row (m, a)
 // holds [u_x | u_y | u_z] blocks of wu[a] columns in the FP32 array at
 // uu_row_ptr[m nu + a] and its pressure columns in the FP64 array at
@@ -56,32 +61,41 @@ __device__ __forceinline__ void gather_unode(const cmfe::KParams& P, const cmfe:
   for (int i = lane; i < 3 * wc; i += 32) acc_c[i] = 0.0;
   double racc = 0.0;
   __syncwarp();
-  const int k1 = u_inc_ptr[a + 1];
-  for (int k = u_inc_ptr[a]; k < k1; ++k) {
-    const int packed = u_inc[k];
-    const int e = packed >> 5, la = packed & 31;
-    const uint16_t* tab = P.tables + ((size_t)P.elem_table[e] * NR + la) * NR;
-    if (lane < NPE) {
-      const int rk = tab[lane] & 0x7fff;
-      const float* src = S.uu + (size_t)e * cmfe::rec_stride_uu(NPE) + (size_t)la * NU3 + lane;
-      float v[9];
-#pragma unroll
-      for (int m = 0; m < 3; ++m)
-#pragma unroll
-        for (int n = 0; n < 3; ++n) v[m * 3 + n] = rec_load<CG>(src + (size_t)m * NPE * NU3 + n * NPE);
-#pragma unroll
-      for (int m = 0; m < 3; ++m)
-#pragma unroll
-        for (int n = 0; n < 3; ++n) acc_u[m * ru + n * wu + rk] += v[m * 3 + n];
+  const int k0 = u_inc_ptr[a], k1 = u_inc_ptr[a + 1];
+  for (int kb = k0; kb < k1; kb += 32) {
+    // up to 32 incidences at once: lane i holds incidence kb + i and its rank-table row
+    const int cnt = min(32, k1 - kb);
+    int pk = 0, trow = 0;
+    if (lane < cnt) {
+      pk = u_inc[kb + lane];
+      trow = P.elem_table[pk >> 5] * NR + (pk & 31);
     }
-    if (lane < NPP) {
-      const int rq = tab[NPE + lane] & 0x7fff;
-      const double* src = S.cp + (size_t)e * cmfe::rec_stride_cp(NPE, NPP) + lane * NU3 + la;
+    for (int j = 0; j < cnt; ++j) {
+      const int packed = __shfl_sync(0xffffffffu, pk, j);
+      const int e = packed >> 5, la = packed & 31;
+      const uint16_t* tab = P.tables + (size_t)__shfl_sync(0xffffffffu, trow, j) * NR;
+      if (lane < NPE) {
+        const int rk = tab[lane] & 0x7fff;
+        const float* src = S.uu + (size_t)e * cmfe::rec_stride_uu(NPE) + (size_t)la * NU3 + lane;
+        float v[9];
 #pragma unroll
-      for (int m = 0; m < 3; ++m) acc_c[m * wc + rq] += rec_load<CG>(src + m * NPE);
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+          for (int n = 0; n < 3; ++n) v[m * 3 + n] = rec_load<CG>(src + (size_t)m * NPE * NU3 + n * NPE);
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+          for (int n = 0; n < 3; ++n) acc_u[m * ru + n * wu + rk] += v[m * 3 + n];
+      }
+      if (lane < NPP) {
+        const int rq = tab[NPE + lane] & 0x7fff;
+        const double* src = S.cp + (size_t)e * cmfe::rec_stride_cp(NPE, NPP) + lane * NU3 + la;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) acc_c[m * wc + rq] += rec_load<CG>(src + m * NPE);
+      }
+      if (lane < 3 && P.r) racc += rec_load<CG>(S.r + (size_t)e * cmfe::rec_stride_r(NPE, NPP) + lane * NPE + la);
+      __syncwarp();
     }
-    if (lane < 3 && P.r) racc += rec_load<CG>(S.r + (size_t)e * cmfe::rec_stride_r(NPE, NPP) + lane * NPE + la);
-    __syncwarp();
   }
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
@@ -106,22 +120,30 @@ __device__ __forceinline__ void gather_pnode(const cmfe::KParams& P, const cmfe:
   for (int i = lane; i < len; i += 32) acc[i] = 0.0;  // pressure-pressure entries stay zero
   double racc = 0.0;
   __syncwarp();
-  const int k1 = p_inc_ptr[q + 1];
-  for (int k = p_inc_ptr[q]; k < k1; ++k) {
-    const int packed = p_inc[k];
-    const int e = packed >> 3, lq = packed & 7;
-    if (lane < NPE) {
-      const uint16_t* tab = P.tables + ((size_t)P.elem_table[e] * NR + NPE + lq) * NR;
-      const int rk = tab[lane] & 0x7fff;
-      const double* src = S.cp + (size_t)e * cmfe::rec_stride_cp(NPE, NPP) + lq * NU3 + lane;
-      double v[3];
-#pragma unroll
-      for (int n = 0; n < 3; ++n) v[n] = rec_load<CG>(src + n * NPE);
-#pragma unroll
-      for (int n = 0; n < 3; ++n) acc[n * wp + rk] += v[n];
+  const int k0 = p_inc_ptr[q], k1 = p_inc_ptr[q + 1];
+  for (int kb = k0; kb < k1; kb += 32) {
+    const int cnt = min(32, k1 - kb);
+    int pk = 0, trow = 0;
+    if (lane < cnt) {
+      pk = p_inc[kb + lane];
+      trow = P.elem_table[pk >> 3] * NR + NPE + (pk & 7);
     }
-    if (lane == 0 && P.r) racc += rec_load<CG>(S.r + (size_t)e * cmfe::rec_stride_r(NPE, NPP) + NU3 + lq);
-    __syncwarp();
+    for (int j = 0; j < cnt; ++j) {
+      const int packed = __shfl_sync(0xffffffffu, pk, j);
+      const int tr = __shfl_sync(0xffffffffu, trow, j);
+      const int e = packed >> 3, lq = packed & 7;
+      if (lane < NPE) {
+        const int rk = P.tables[(size_t)tr * NR + lane] & 0x7fff;
+        const double* src = S.cp + (size_t)e * cmfe::rec_stride_cp(NPE, NPP) + lq * NU3 + lane;
+        double v[3];
+#pragma unroll
+        for (int n = 0; n < 3; ++n) v[n] = rec_load<CG>(src + n * NPE);
+#pragma unroll
+        for (int n = 0; n < 3; ++n) acc[n * wp + rk] += v[n];
+      }
+      if (lane == 0 && P.r) racc += rec_load<CG>(S.r + (size_t)e * cmfe::rec_stride_r(NPE, NPP) + NU3 + lq);
+      __syncwarp();
+    }
   }
   double* dc = P.vals + P.cp_row_ptr[row];
   for (int i = lane; i < len; i += 32) dc[i] = acc[i];

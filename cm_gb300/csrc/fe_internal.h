@@ -61,6 +61,10 @@ struct HostSetup {
   // node (sorted by element number, packed e * 32 + local node) and around
   // every pressure row node (e * 8 + local pressure node).
   std::vector<int32_t> u_inc_ptr, u_inc, p_inc_ptr, p_inc;
+  // the largest element number around any of the row nodes 0..a (u nodes)
+  // and 0..q (pressure row nodes): once the elements below E are assembled,
+  // every node a with u_last_prefix[a] < E has its rows complete
+  std::vector<int32_t> u_last_prefix, p_last_prefix;
   // shared memory one gather warp needs: the larger of a u node's three rows
   // (3 x 3 wu FP32, then 3 x its pressure columns FP64) and a pressure row (FP64)
   int gather_bytes = 0;
@@ -133,9 +137,10 @@ struct FusedArgs {
   const int32_t* u_inc;
   const int32_t* p_inc_ptr;
   const int32_t* p_inc;
-  int* work;
+  int* work;       // this launch's group counter
   int* node_done;
   const uint8_t* bmask;
+  int g0, g1;      // element groups of this launch: [g0, g1)
   int gwarps;  // warps that gather (set by the launcher)
   int gbytes;  // scratch bytes per gathering warp (set by the launcher)
 };
@@ -144,6 +149,9 @@ struct FusedArgs {
 // with the high-precision phases in FP64 or in double-float arithmetic.
 // Returns a cudaError_t value.
 int launch_mixed(const HostSetup& s, const KParams& kp, int num_sms, void* stream, bool double_float);
+
+// Elements per group of the fused kernel for this element type.
+int fused_group_size(const HostSetup& s);
 
 // Launches the mixed-precision assembly kernel over all elements with its
 // output staged per element (so; fe_mixed.cu), in

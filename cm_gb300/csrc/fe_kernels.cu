@@ -498,7 +498,12 @@ struct fe_equations_set {
   int32_t *d_u_inc_ptr = nullptr, *d_u_inc = nullptr, *d_p_inc_ptr = nullptr, *d_p_inc = nullptr;
   float* d_st_uu = nullptr;
   double *d_st_cp = nullptr, *d_st_r = nullptr;
-  int* d_fuse = nullptr;  // fused staged assembly: [0] work counter, [1 ..] per-row-node counts
+  int* d_fuse = nullptr;  // fused staged assembly: [0, kFuseChunks) group counters, then per-row-node counts
+  int host_output = FE_HOST_OUTPUT_STREAMED;
+  int stream_chunks = 0;  // launches of a streamed assembly; 0: by the output size
+  // streamed host outputs: the copy stream and one event per chunk (+ the last copy)
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> chunk_events;
   unsigned* d_status = nullptr;
   int32_t* d_col = nullptr;  // CSR columns on the device, uploaded on first use (Newton driver)
   // staging for calls given host memory
@@ -609,51 +614,87 @@ int surface_after(fe_handle h, const KParams& kp, int c, int want_jac, cudaStrea
   return FE_NO_ERROR;
 }
 
-// The staged mixed assembly into device buffers: one launch over all
-// elements into the per-element records, the surface-pressure faces added to
-// the records of their elements, then the row gather.  Adds the number of
-// kernels launched to *count when count is set.
 int ensure(void** buf, size_t bytes);
 
-int mixed_staged(fe_handle h, const double* dx, float* du, double* dc, double* dr, bool double_float,
-                 cudaStream_t st, int64_t* count) {
+// Group counters at the head of d_fuse: the most launches one fused assembly
+// is split into.
+constexpr int kFuseChunks = 64;
+// The most chunks a streamed assembly is split into.
+constexpr int kStreamChunks = 16;
+
+// The fused staged assembly (element records and row gathers in one kernel)
+// in `chunks` launches over consecutive ranges of element groups; when `done`
+// is given, done[c] is recorded on the stream after launch c.  The per-node
+// counts run on across the launches: a node's rows are gathered by the launch
+// that assembles the last element around it.
+int mixed_fused(fe_handle h, const KParams& kp, const cmfe::StageOut& so, bool double_float, cudaStream_t st,
+                int chunks, cudaEvent_t* done, int64_t* count) {
+  const auto& s = h->hs;
+  int rc;
+  const size_t counters = kFuseChunks + (size_t)s.nu + (size_t)s.npn;
+  if ((rc = ensure((void**)&h->d_fuse, sizeof(int) * counters))) return rc;
+  CUDA_TRY(cudaMemsetAsync(h->d_fuse, 0, sizeof(int) * counters, st));
+  const int nb = s.bnd_ptr.empty() ? 0 : s.bnd_ptr[s.ncolours];
+  const int64_t groups = (s.ne + cmfe::fused_group_size(s) - 1) / cmfe::fused_group_size(s);
+  chunks = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)chunks, (int64_t)kFuseChunks, groups}));
+  cmfe::FusedArgs fa;
+  std::memset(&fa, 0, sizeof(fa));
+  fa.u_inc_ptr = h->d_u_inc_ptr;
+  fa.u_inc = h->d_u_inc;
+  fa.p_inc_ptr = h->d_p_inc_ptr;
+  fa.p_inc = h->d_p_inc;
+  fa.node_done = h->d_fuse + kFuseChunks;
+  fa.bmask = h->has_surfp && nb > 0 ? h->d_bnd_mask : nullptr;
+  for (int c = 0; c < chunks; ++c) {
+    fa.work = h->d_fuse + c;
+    fa.g0 = (int)(groups * c / chunks);
+    fa.g1 = (int)(groups * (c + 1) / chunks);
+    const int e = cmfe::launch_mixed_fused(s, kp, so, fa, h->num_sms, st, double_float);
+    if (e != 0)
+      return set_error(FE_ERR_CUDA, std::string("fused kernel launch: ") + cudaGetErrorString((cudaError_t)e));
+    if (done) CUDA_TRY(cudaEventRecord(done[c], st));
+  }
+  h->launches += chunks;
+  if (count) *count += chunks;
+  return FE_NO_ERROR;
+}
+
+int ensure_records(fe_handle h) {
   const auto& s = h->hs;
   int rc;
   if ((rc = ensure((void**)&h->d_st_uu, sizeof(float) * cmfe::rec_stride_uu(s.npe) * (size_t)s.ne)) ||
       (rc = ensure((void**)&h->d_st_cp, sizeof(double) * cmfe::rec_stride_cp(s.npe, s.npp) * (size_t)s.ne)) ||
       (rc = ensure((void**)&h->d_st_r, sizeof(double) * cmfe::rec_stride_r(s.npe, s.npp) * (size_t)s.ne)))
     return rc;
+  return FE_NO_ERROR;
+}
+
+KParams staged_params(fe_handle h, const double* dx, float* du, double* dc, double* dr) {
   KParams kp = base_params(h);
   kp.x = dx;
   kp.vals_uu = du;
   kp.vals = dc;
   kp.r = dr;
-  const cmfe::StageOut so{h->d_st_uu, h->d_st_cp, h->d_st_r};
   kp.elems = nullptr;
   kp.first_elem = 0;
-  kp.count = s.ne;
+  kp.count = h->hs.ne;
+  return kp;
+}
+
+// The staged mixed assembly into device buffers: one launch over all
+// elements into the per-element records, the surface-pressure faces added to
+// the records of their elements, then the row gather (or all three in the
+// fused kernel where its gather scratch fits).  Adds the number of kernels
+// launched to *count when count is set.
+int mixed_staged(fe_handle h, const double* dx, float* du, double* dc, double* dr, bool double_float,
+                 cudaStream_t st, int64_t* count) {
+  const auto& s = h->hs;
+  int rc;
+  if ((rc = ensure_records(h))) return rc;
+  const KParams kp = staged_params(h, dx, du, dc, dr);
+  const cmfe::StageOut so{h->d_st_uu, h->d_st_cp, h->d_st_r};
+  if (cmfe::fused_fits(s)) return mixed_fused(h, kp, so, double_float, st, 1, nullptr, count);
   const int nb = s.bnd_ptr.empty() ? 0 : s.bnd_ptr[s.ncolours];
-  if (cmfe::fused_fits(s)) {
-    // one launch: element records and row gathers together
-    const size_t counters = 1 + (size_t)s.nu + (size_t)s.npn;
-    if ((rc = ensure((void**)&h->d_fuse, sizeof(int) * counters))) return rc;
-    CUDA_TRY(cudaMemsetAsync(h->d_fuse, 0, sizeof(int) * counters, st));
-    cmfe::FusedArgs fa;
-    std::memset(&fa, 0, sizeof(fa));
-    fa.u_inc_ptr = h->d_u_inc_ptr;
-    fa.u_inc = h->d_u_inc;
-    fa.p_inc_ptr = h->d_p_inc_ptr;
-    fa.p_inc = h->d_p_inc;
-    fa.work = h->d_fuse;
-    fa.node_done = h->d_fuse + 1;
-    fa.bmask = h->has_surfp && nb > 0 ? h->d_bnd_mask : nullptr;
-    const int e = cmfe::launch_mixed_fused(s, kp, so, fa, h->num_sms, st, double_float);
-    if (e != 0)
-      return set_error(FE_ERR_CUDA, std::string("fused kernel launch: ") + cudaGetErrorString((cudaError_t)e));
-    h->launches += 1;
-    if (count) *count += 1;
-    return FE_NO_ERROR;
-  }
   int e = cmfe::launch_mixed_staged(s, kp, so, h->num_sms, st, double_float);
   if (e != 0) return set_error(FE_ERR_CUDA, std::string("staged kernel launch: ") + cudaGetErrorString((cudaError_t)e));
   int64_t n = 1;
@@ -667,6 +708,72 @@ int mixed_staged(fe_handle h, const double* dx, float* du, double* dc, double* d
   ++n;
   h->launches += n;
   if (count) *count += n;
+  return FE_NO_ERROR;
+}
+
+// Streamed host outputs: the fused assembly in chunks of element groups into
+// the device buffers du / dc / dr; after each chunk, the rows it completed --
+// the leading u nodes and pressure row nodes whose elements are all assembled,
+// in each of the row blocks -- are copied to the host outputs hu / hc / hr
+// (NULL: that output is device memory, written directly) on a copy stream,
+// while the next chunks assemble.  The caller's stream waits for the last copy.
+int mixed_streamed(fe_handle h, const double* dx, float* du, double* dc, double* dr, float* hu, double* hc,
+                   double* hr, bool double_float, cudaStream_t st) {
+  const auto& s = h->hs;
+  int rc;
+  if ((rc = ensure_records(h))) return rc;
+  const int64_t groups = (s.ne + cmfe::fused_group_size(s) - 1) / cmfe::fused_group_size(s);
+  const size_t host_bytes = (hu ? sizeof(float) * (size_t)s.nnz_uu : 0) +
+                            (hc ? sizeof(double) * (size_t)s.nnz_cp : 0) + (hr ? sizeof(double) * (size_t)s.ndofs : 0);
+  // chunks of about 48 MB of output: small enough that the last copy, which
+  // nothing overlaps, is short; few enough that each launch's tail is too
+  const int64_t want = h->stream_chunks > 0 ? h->stream_chunks : (int64_t)(host_bytes / (48u << 20)) + 1;
+  const int chunks = (int)std::max<int64_t>(1, std::min<int64_t>({want, (int64_t)kStreamChunks, groups}));
+  if (!h->copy_stream) CUDA_TRY(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+  while ((int)h->chunk_events.size() < kStreamChunks + 1) {
+    cudaEvent_t ev;
+    CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    h->chunk_events.push_back(ev);
+  }
+  const KParams kp = staged_params(h, dx, du, dc, dr);
+  const cmfe::StageOut so{h->d_st_uu, h->d_st_cp, h->d_st_r};
+  cudaEvent_t* ev = h->chunk_events.data();
+  if ((rc = mixed_fused(h, kp, so, double_float, st, chunks, ev, nullptr))) return rc;
+  cudaStream_t cs = h->copy_stream;
+  const int nu = s.nu, npn = s.npn, EG = cmfe::fused_group_size(s);
+  auto copy_rows = [&](int64_t r0, int64_t r1) -> int {
+    if (r1 <= r0) return FE_NO_ERROR;
+    if (hu && r0 < 3 * (int64_t)nu) {
+      const int64_t a = s.uu_row_ptr[r0], b = s.uu_row_ptr[r1];
+      if (b > a) CUDA_TRY(cudaMemcpyAsync(hu + a, du + a, sizeof(float) * (b - a), cudaMemcpyDeviceToHost, cs));
+    }
+    if (hc) {
+      const int64_t a = s.cp_row_ptr[r0], b = s.cp_row_ptr[r1];
+      if (b > a) CUDA_TRY(cudaMemcpyAsync(hc + a, dc + a, sizeof(double) * (b - a), cudaMemcpyDeviceToHost, cs));
+    }
+    if (hr) CUDA_TRY(cudaMemcpyAsync(hr + r0, dr + r0, sizeof(double) * (r1 - r0), cudaMemcpyDeviceToHost, cs));
+    return FE_NO_ERROR;
+  };
+  int a0 = 0, q0 = 0;
+  for (int c = 0; c < chunks; ++c) {
+    const int64_t end = std::min<int64_t>(groups * (c + 1) / chunks * EG, s.ne);  // elements assembled
+    int a1 = nu, q1 = npn;
+    if (c + 1 < chunks) {
+      a1 = (int)(std::upper_bound(s.u_last_prefix.begin(), s.u_last_prefix.end(), (int32_t)(end - 1)) -
+                 s.u_last_prefix.begin());
+      q1 = (int)(std::upper_bound(s.p_last_prefix.begin(), s.p_last_prefix.end(), (int32_t)(end - 1)) -
+                 s.p_last_prefix.begin());
+    }
+    if (a1 == a0 && q1 == q0) continue;
+    CUDA_TRY(cudaStreamWaitEvent(cs, ev[c], 0));
+    for (int m = 0; m < 3; ++m)
+      if ((rc = copy_rows((int64_t)m * nu + a0, (int64_t)m * nu + a1))) return rc;
+    if ((rc = copy_rows(3 * (int64_t)nu + q0, 3 * (int64_t)nu + q1))) return rc;
+    a0 = a1;
+    q0 = q1;
+  }
+  CUDA_TRY(cudaEventRecord(ev[kStreamChunks], cs));
+  CUDA_TRY(cudaStreamWaitEvent(st, ev[kStreamChunks], 0));
   return FE_NO_ERROR;
 }
 
@@ -1055,6 +1162,9 @@ int fe_destroy(fe_handle h) {
                  h->d_col, h->d_st_uu, h->d_st_cp, h->d_st_r, h->d_fuse};
   for (void* p : own)
     if (p) cudaFree(p);
+  for (cudaEvent_t ev : h->chunk_events)
+    if (ev) cudaEventDestroy(ev);
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   delete h;  // releases this handle's share of the mesh arrays
   return FE_NO_ERROR;
 }
@@ -1095,6 +1205,8 @@ int fe_clone(fe_handle src, fe_handle* out) {
     h->d_p_inc = src->d_p_inc;
     h->high_precision = src->high_precision;
     h->assembly_order = src->assembly_order;
+    h->host_output = src->host_output;
+    h->stream_chunks = src->stream_chunks;
   }
   auto fail = [&](int code) {
     fe_destroy(h);
@@ -1291,7 +1403,20 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
   double* dc = values_coupling;
   double* dr = r;
   bool mapped_out = false;  // some output is host memory written in place: wait before returning
-  if (h->assembly_order == FE_ASSEMBLY_STAGED && h->hs.gather_bytes > 0) {
+  const bool staged = h->assembly_order == FE_ASSEMBLY_STAGED && h->hs.gather_bytes > 0;
+  if (staged && (hu || hc || hr) && h->host_output == FE_HOST_OUTPUT_STREAMED && cmfe::fused_fits(h->hs)) {
+    // the rows each chunk of elements completes go to the host while the
+    // next chunks assemble
+    if (hu && (rc = ensure((void**)&h->s_uu, sizeof(float) * h->hs.nnz_uu))) return rc;
+    if (hc && (rc = ensure((void**)&h->s_cp, sizeof(double) * h->hs.nnz_cp))) return rc;
+    if (hr && (rc = ensure((void**)&h->s_r, sizeof(double) * h->hs.ndofs))) return rc;
+    if ((rc = mixed_streamed(h, dx, hu ? h->s_uu : values_uu, hc ? h->s_cp : values_coupling, hr ? h->s_r : r,
+                             hu ? values_uu : nullptr, hc ? values_coupling : nullptr, hr ? r : nullptr,
+                             h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT, st)))
+      return rc;
+    return finish_status(h, st);
+  }
+  if (staged && h->host_output == FE_HOST_OUTPUT_IN_PLACE) {
     // the row gather writes each output row once, contiguously: page-locked
     // host outputs are written in place over the host link, with no device
     // copy of the result and no separate device-to-host copy
@@ -1413,6 +1538,17 @@ int fe_set_assembly_order(fe_handle h, int32_t order) {
     return set_error(FE_ERR_INVALID_ARGUMENT, "unknown assembly order");
   std::lock_guard<std::mutex> lk(h->mu);
   h->assembly_order = order;
+  return FE_NO_ERROR;
+}
+
+int fe_set_host_output(fe_handle h, int32_t mode, int32_t chunks) {
+  if (!h) return set_error(FE_ERR_INVALID_ARGUMENT, "NULL handle");
+  if (mode != FE_HOST_OUTPUT_STREAMED && mode != FE_HOST_OUTPUT_IN_PLACE && mode != FE_HOST_OUTPUT_AFTER)
+    return set_error(FE_ERR_INVALID_ARGUMENT, "unknown host output mode");
+  if (chunks < 0 || chunks > kStreamChunks) return set_error(FE_ERR_INVALID_ARGUMENT, "chunks must be 0..16");
+  std::lock_guard<std::mutex> lk(h->mu);
+  h->host_output = mode;
+  h->stream_chunks = chunks;
   return FE_NO_ERROR;
 }
 

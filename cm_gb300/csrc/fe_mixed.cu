@@ -51,14 +51,14 @@ __global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB)
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ int s_grp, s_nready;
   mix_tables<N1, PM, EG, H>(P, sm);
-  const int ngroups = (P.count + EG - 1) / EG;
+  const int ngroups = min((P.count + EG - 1) / EG, F.g1);
   const bool p4_first = (blockIdx.x / P.wave) & 1;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int* s_node = reinterpret_cast<const int*>(sm + C::O_NODE);
   int* ready = reinterpret_cast<int*>(sm + C::O_READY);
   unsigned char* scratch = sm + C::O_SCRATCH;
   for (;;) {
-    if (tid == 0) s_grp = atomicAdd(F.work, 1);
+    if (tid == 0) s_grp = F.g0 + atomicAdd(F.work, 1);
     __syncthreads();
     const int grp = s_grp;
     if (grp >= ngroups) break;
@@ -126,7 +126,10 @@ int launch_fused_t(const KParams& kp, const cmfe::StageOut& so, cmfe::FusedArgs 
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::THREADS, C::SMEM);
   if (e != cudaSuccess) return (int)e;
   per_sm = per_sm < 1 ? 1 : per_sm;
-  const int groups = (kp.count + C::EG - 1) / C::EG;
+  const int all = (kp.count + C::EG - 1) / C::EG;
+  if (fa.g1 > all) fa.g1 = all;
+  if (fa.g0 < 0 || fa.g0 >= fa.g1) return (int)cudaSuccess;  // no groups in this launch
+  const int groups = fa.g1 - fa.g0;
   int grid = per_sm * num_sms;
   grid = grid < groups ? grid : groups;
   grid = grid < 1 ? 1 : grid;
@@ -194,6 +197,11 @@ int launch_mixed(const HostSetup& s, const KParams& kp, int num_sms, void* strea
   cudaStream_t st = (cudaStream_t)stream;
   if (kp.count <= 0) return 0;
   return double_float ? launch_h<dd>(s, kp, num_sms, st) : launch_h<double>(s, kp, num_sms, st);
+}
+
+int fused_group_size(const HostSetup& s) {
+  if (s.n1 == 2) return s.pmode ? MixCfg<2, 1>::EG : MixCfg<2, 0>::EG;
+  return s.pmode ? MixCfg<3, 1>::EG : MixCfg<3, 0>::EG;
 }
 
 int fused_fits(const HostSetup& s) {

@@ -257,6 +257,18 @@ int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg) {
     }
   });
 
+  // Completion order of the rows: the largest element around nodes 0..a.
+  s.u_last_prefix.resize(s.nu);
+  s.p_last_prefix.resize(s.npn);
+  for (int n = 0, m = -1; n < s.nu; ++n) {
+    if (!surr_u[n].empty()) m = std::max(m, surr_u[n].back());
+    s.u_last_prefix[n] = m;
+  }
+  for (int q = 0, m = -1; q < s.npn; ++q) {
+    if (!surr_p[q].empty()) m = std::max(m, surr_p[q].back());
+    s.p_last_prefix[q] = m;
+  }
+
   // Neighbourhoods: sorted u nodes and sorted pressure row nodes around every row node.
   std::vector<std::vector<int32_t>> nbu_u(s.nu), nbp_u(s.nu), nbu_p(s.npn), nbp_p(s.npn);
   auto fill_nb = [&](const std::vector<int32_t>& elems, std::vector<int32_t>& nu_out, std::vector<int32_t>& np_out) {

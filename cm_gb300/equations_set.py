@@ -242,6 +242,18 @@ class FiniteElasticityEquationsSet:
         check(_lib.load().fe_set_assembly_order(self._h, code))
         self.assembly_order = order
 
+    def set_host_output(self, mode, chunks=0):
+        """fe_set_host_output: how jacobian_evaluate_mixed delivers outputs in
+        host memory -- "streamed" (the default: rows copied to the host chunk
+        by chunk while the rest assembles; `chunks` launches, 0 = by size),
+        "in_place" (page-locked outputs written by the row gather over the
+        host link) or "after" (one copy after the assembly).  The values are
+        identical in every mode."""
+        code = {"streamed": _lib.FE_HOST_OUTPUT_STREAMED, "in_place": _lib.FE_HOST_OUTPUT_IN_PLACE,
+                "after": _lib.FE_HOST_OUTPUT_AFTER}[mode]
+        check(_lib.load().fe_set_host_output(self._h, code, chunks))
+        self.host_output = mode
+
     def newton_load_step(self, x, fixed_dofs, fixed_values, **options):
         """fe_newton_load_step: one load increment by Newton on the device
         (FP64 Jacobian, block-diagonal-preconditioned GMRES, cubic

@@ -11,11 +11,15 @@ finite_elasticity_routines.f90:1075-1153).  It is preconditioned by the block
 lower-triangular operator [A 0; B -S] with
 
 * A^-1 ~ one V-cycle of geometric multigrid on the displacement block:
-  Galerkin coarse operators A_c = P^T A P on a hierarchy of regular grids
-  (triquadratic -> trilinear on the element vertices, then trilinear with the
-  element count halved per direction), Chebyshev smoothing on the Jacobi-
-  scaled operator, the inverse of the coarsest operator (dense); on the GPU
-  one V-cycle is recorded in a CUDA graph and replayed;
+  coarse operators on a hierarchy of regular grids (triquadratic -> trilinear
+  on the element vertices, then trilinear with the element count halved per
+  direction), Chebyshev smoothing on the Jacobi-scaled operator, the inverse
+  of the coarsest operator (dense); on the GPU one V-cycle is recorded in a
+  CUDA graph and replayed.  The first coarse operator of a triquadratic mesh
+  is either the Galerkin product P^T A P or, cheaper at large sizes, the
+  displacement block of the trilinear mesh on the element vertices assembled
+  at the injected state (rediscretisation; `vertex_mesh`); the further
+  levels are Galerkin products;
 * S ~ the consistent pressure mass matrix times a scale taken from
   diag(B diag(A)^-1 B^T) of the current Jacobian (the mass matrix is
   spectrally equivalent to the Schur complement for inf-sup stable pairs),
@@ -80,6 +84,68 @@ def grid_hierarchy(grid_u, nxi_u, min_dofs=1500):
     return levels
 
 
+def vertex_mesh(mesh):
+    """The trilinear box mesh on the element vertices of a triquadratic box
+    mesh: the same elements (same numbering), the vertex coordinates and
+    fibre angles of the fine mesh, the same materials and pressure
+    interpolation.  Returns the mesh and, per coarse dof, the fine dof it
+    takes its value from (injection; nodal pressure lives on the vertices in
+    both meshes, numbered alike)."""
+    import dataclasses
+
+    from .mesh import FE_PRESSURE_NODE_BASED, regular_box
+    if mesh.nxi_u != 3 or not mesh.grid_u:
+        raise ValueError("vertex_mesh needs a triquadratic box mesh")
+    ex, ey, ez = mesh.dims
+    n1, n2, _ = mesh.grid_u
+    node = mesh.p_mode == FE_PRESSURE_NODE_BASED
+    cm = regular_box(ex, ey, ez, lengths=mesh.lengths, nxi_u=2, pressure="node" if node else "element",
+                     law=mesh.law, materials=mesh.materials)
+    ci = np.arange(cm.nu)
+    cx, cy, cz = ci % (ex + 1), (ci // (ex + 1)) % (ey + 1), ci // ((ex + 1) * (ey + 1))
+    vid = 2 * cx + n1 * (2 * cy + n2 * 2 * cz)
+    fib = None if mesh.fibre is None else np.ascontiguousarray(mesh.fibre[:, vid])
+    cm = dataclasses.replace(cm, X=np.ascontiguousarray(mesh.X[:, vid]), fibre=fib,
+                             materials=np.array(mesh.materials, dtype=np.float64, copy=True))
+    nuf = mesh.nu
+    inj = [c * nuf + vid for c in range(3)]
+    inj.append(3 * nuf + np.arange(cm.n_pressure))
+    return cm, np.concatenate(inj).astype(np.int64)
+
+
+class VertexOperator:
+    """The first coarse operator of a triquadratic box mesh by
+    rediscretisation: the free displacement block of the Jacobian of
+    `vertex_mesh(mesh)`, assembled by `coarse_es` (an equations set of that
+    mesh) at the state injected from the fine one.  free_c is the mask of
+    free coarse displacement dofs (the multigrid's level-1 mask)."""
+
+    def __init__(self, mesh, coarse_es, free_c, device):
+        self.es = coarse_es
+        self.device = torch.device(device)
+        cm = coarse_es.mesh
+        self.inj = torch.from_numpy(vertex_mesh(mesh)[1]).to(self.device)
+        rp, col = coarse_es.csr_pattern()
+        rp, col = rp.astype(np.int64), col.astype(np.int64)
+        nu3 = 3 * cm.nu
+        free = np.zeros(cm.ndofs, dtype=bool)
+        free[:nu3] = free_c
+        row = np.repeat(np.arange(cm.ndofs), np.diff(rp))
+        keep = free[row] & free[col]
+        new = np.cumsum(free) - 1
+        counts = np.bincount(new[row[keep]], minlength=int(free.sum()))
+        self.sel = torch.from_numpy(np.nonzero(keep)[0]).to(self.device)
+        self.crow = torch.from_numpy(np.concatenate([[0], np.cumsum(counts)])).to(self.device)
+        self.col = torch.from_numpy(new[col[keep]]).to(self.device)
+        self.n = int(free.sum())
+        self.vals = torch.empty(coarse_es.nnz, dtype=torch.float64, device=self.device)
+
+    def assemble(self, x, dtype):
+        """The coarse operator at the fine state x (full dof vector)."""
+        self.es.jacobian_evaluate(x[self.inj].contiguous(), self.vals)
+        return torch.sparse_csr_tensor(self.crow, self.col, self.vals[self.sel].to(dtype), size=(self.n, self.n))
+
+
 class BoxMultigrid:
     """V-cycle for the free displacement block of a regular box mesh.
 
@@ -91,6 +157,7 @@ class BoxMultigrid:
         self.levels = grid_hierarchy(grid_u, nxi_u, min_dofs)
         self.P, self.R = [], []
         free = np.asarray(free_u, dtype=bool)
+        self.free = [free]
         for lf, lc in zip(self.levels[:-1], self.levels[1:]):
             p1 = [_interp1d(nf, nc) for nf, nc in zip(lf, lc)]
             P3 = sp.kron(p1[2], sp.kron(p1[1], p1[0], format="csr"), format="csr")
@@ -106,14 +173,20 @@ class BoxMultigrid:
             self.P.append(_to_torch_csr(Pf, device, dtype))
             self.R.append(_to_torch_csr(Pf.T, device, dtype))
             free = cfree
+            self.free.append(free)
         self.n_coarse = int(free.sum())
 
     # ------------------------------------------------------------------ setup
-    def setup(self, A):
-        """A: free displacement block, torch CSR on the device (any float dtype)."""
+    def setup(self, A, A1=None):
+        """A: free displacement block, torch CSR on the device (any float
+        dtype); A1 (optional): the first coarse operator, else the Galerkin
+        product."""
         A = A.to(self.dtype)
         self.A = [A]
-        for P, R in zip(self.P, self.R):
+        for lvl, (P, R) in enumerate(zip(self.P, self.R)):
+            if lvl == 0 and A1 is not None:
+                self.A.append(A1.to(self.dtype))
+                continue
             Ac = torch.sparse.mm(R, torch.sparse.mm(self.A[-1], P))
             self.A.append(Ac.to_sparse_csr())
         self.dinv, self.lmax = [], []

@@ -46,6 +46,8 @@ class NewtonOptions:
     gmres_restart: int = 30      # GMRES(30), relative tolerance 1e-5
     gmres_max_iterations: int = 600
     forcing: str = "constant"    # "constant" (gmres_rtol) or "ew" (Eisenstat-Walker choice 2)
+    mg_coarse: str = "vertex"    # first coarse operator of a triquadratic mesh: "vertex" (the trilinear
+    #                              vertex mesh assembled at the injected state) or "galerkin" (P^T A P)
 
 
 @dataclass
@@ -59,6 +61,7 @@ class StepReport:
     seconds: float = 0.0
     assembly_seconds: float = 0.0
     linear_seconds: float = 0.0
+    preconditioner_seconds: float = 0.0  # part of linear_seconds: multigrid set-up
 
 
 class DirichletConditions:
@@ -249,12 +252,19 @@ class LoadStepSolver:
             m = es.mesh
             self.mg = BoxMultigrid(m.grid_u, m.nxi_u, self.free_mask[:3 * m.nu], self.device,
                                    torch.float32 if self.opt.precision == "mixed" else torch.float64)
+            self.coarse = None
+            if self.opt.mg_coarse == "vertex" and m.nxi_u == 3 and len(self.mg.free) > 1:
+                from .multigrid import VertexOperator, vertex_mesh
+                cm, _ = vertex_mesh(m)
+                self.coarse = VertexOperator(m, type(es)(cm), self.mg.free[1], self.device)
+                self.coarse_materials = None
             fp = self.free_mask[3 * m.nu:]
             Mp = pressure_mass_matrix(m)[fp][:, fp]
             self.mass_p = torch.from_numpy(Mp.diagonal().copy()).to(self.device)
             self.mass_solver = MassSolver(Mp, self.device)
         self.vals = torch.empty(es.nnz, dtype=torch.float64, device=self.device)
         self.r = torch.empty(es.ndofs, dtype=torch.float64, device=self.device)
+        self.setup_seconds = 0.0
 
     def _sync(self):
         if self.device.type == "cuda":
@@ -292,6 +302,7 @@ class LoadStepSolver:
         return self.r[self.sys.free]
 
     def jacobian(self, x):
+        self._x_jac = x  # the state of the Jacobian (the multigrid's coarse operator is assembled there)
         if self.opt.precision == "mixed":
             self.es.jacobian_evaluate_mixed(x, self.vu, self.vc, self.r)
             self.vals[self.uu_pos] = self.vu.double()
@@ -322,9 +333,18 @@ class LoadStepSolver:
         """Block lower-triangular preconditioner [A 0; B -S]^-1 with a multigrid
         V-cycle for A and the scaled lumped pressure mass for S."""
         S = self.sys
+        t0 = time.perf_counter()
         mg_dtype = torch.float32 if self.opt.precision == "mixed" else torch.float64
         A, B = S.blocks(J, mg_dtype)
-        self.mg.setup(A)
+        A1 = None
+        if self.coarse is not None:
+            mats = getattr(self.es, "materials", None)
+            mats = self.es.mesh.materials if mats is None else mats
+            if self.coarse_materials is None or not np.array_equal(mats, self.coarse_materials):
+                self.coarse.es.set_materials(mats)
+                self.coarse_materials = np.array(mats, copy=True)
+            A1 = self.coarse.assemble(self._x_jac, mg_dtype)
+        self.mg.setup(A, A1)
         dA = self.mg.dinv[0].to(torch.float64)
         sd = torch.zeros(S.nfp, dtype=torch.float64, device=self.device)
         bv = B.values()
@@ -332,6 +352,7 @@ class LoadStepSolver:
         sd.index_add_(0, brow, bv * bv * dA[B.col_indices()])
         scale = float(torch.median(sd / self.mass_p))
         nfu = S.nfu
+        self.setup_seconds += time.perf_counter() - t0
 
         def apply(w):
             zu = self.mg.vcycle(w[:nfu].to(mg_dtype)).to(torch.float64)
@@ -383,10 +404,12 @@ class LoadStepSolver:
                     eta = max(eta, 0.9 * prev_eta ** 2)
                 eta = min(max(eta, o.gmres_rtol), 0.5)
                 prev_eta = eta
+            self.setup_seconds = 0.0
             d, lin_it = self.linear_solve(A, -r, eta)
             self._sync()
             rep.assembly_seconds += tb - ta
             rep.linear_seconds += time.perf_counter() - tb
+            rep.preconditioner_seconds += self.setup_seconds
             rep.linear_iterations.append(int(lin_it))
             dn = float(d.norm())
             if dn > o.max_step:
@@ -445,11 +468,13 @@ class LoadStepSolver:
         rep.seconds = time.perf_counter() - t_start
         return x, rep
 
-    def solve(self, x0, increments: int, guesses=None, pressure: PressureIncrements | None = None):
+    def solve(self, x0, increments: int, guesses=None, pressure: PressureIncrements | None = None,
+              progress=None):
         """All load increments from state x0; guesses (optional) maps the
         increment number to a Newton initial guess for the free dofs;
         pressure (optional) raises a surface-pressure load with the
-        increments."""
+        increments; progress (optional) is called with (increment, report)
+        after each increment."""
         x = x0.clone()
         reports = []
         for i in range(1, increments + 1):
@@ -460,6 +485,8 @@ class LoadStepSolver:
                 x[self.sys.free] = guesses[i][self.sys.free]
             x, rep = self.newton(x)
             reports.append(rep)
+            if progress is not None:
+                progress(i, rep)
             if not rep.converged:
                 break
         return x, reports

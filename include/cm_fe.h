@@ -132,12 +132,9 @@ int fe_jacobian_evaluate(fe_handle h, const double* x, double* values, double* r
  * pressure-pressure block) in FP64.  The two value arrays follow the split
  * pattern returned by fe_mixed_layout().  If r is not NULL the FP64 residual
  * at x is produced by the same pass.  No counterpart in the reference (which
- * assembles in FP64 only); its FP64 parts match fe_jacobian_evaluate.  In
- * the staged assembly order (fe_set_assembly_order), outputs in page-locked
- * host memory (cudaHostAlloc / cudaHostRegister) are written in place by the
- * row gather over the host link, without a device copy of the result; other
- * host memory goes through staging buffers.  Either way the call returns
- * after the host outputs are written. */
+ * assembles in FP64 only); its FP64 parts match fe_jacobian_evaluate.
+ * Outputs in host memory are delivered as fe_set_host_output selects; the
+ * call returns after they are written. */
 int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, double* values_coupling,
                                double* r, void* stream);
 
@@ -193,11 +190,12 @@ int fe_set_high_precision(fe_handle h, int32_t mode);
  * CSR values and the residual (both deterministic; no counterpart in the
  * reference, which adds element by element, MATRIX_VALUES_ADD_DP2,
  * matrix_vector.f90:2756-2880).
- * FE_ASSEMBLY_STAGED (the default): one launch evaluates every element and
- * stores its entries in per-element records on the device; a second kernel
- * then forms each CSR row once from the records of the elements around the
- * row's node, in increasing element number.  Every matrix sector is written
- * once and never read.  The records take, per element, 4 (3 n_p)^2 +
+ * FE_ASSEMBLY_STAGED (the default): every element stores its entries in a
+ * per-element record on the device, and each CSR row is formed once from the
+ * records of the elements around the row's node, in increasing element
+ * number: in the same launch, by the block that assembles the node's last
+ * element (where one row node's rows fit that kernel's shared memory), else
+ * by a second kernel.  Every matrix sector is written once and never read.  The records take, per element, 4 (3 n_p)^2 +
  * 8 n_q 3 n_p + 8 (3 n_p + n_q) bytes (32 kB for a triquadratic element with
  * nodal pressure), allocated on the first staged evaluation and kept with
  * the handle.
@@ -209,6 +207,26 @@ int fe_set_high_precision(fe_handle h, int32_t mode);
 #define FE_ASSEMBLY_STAGED 0
 #define FE_ASSEMBLY_COLOURED 1
 int fe_set_assembly_order(fe_handle h, int32_t order);
+
+/* How fe_jacobian_evaluate_mixed delivers outputs that are in host memory
+ * (no counterpart in the reference, whose matrices live in host memory).
+ * FE_HOST_OUTPUT_STREAMED (the default; staged order): the assembly runs in
+ * up to 16 launches over consecutive ranges of elements; after each, the rows
+ * whose elements are all assembled (for a mesh numbered like the elements,
+ * the leading rows of each row block) are copied to the host on a second
+ * stream while the next launches run.  Device staging for the outputs.
+ * FE_HOST_OUTPUT_IN_PLACE (staged order): outputs in page-locked host memory
+ * (cudaHostAlloc / cudaHostRegister) are written in place by the row gather
+ * over the host link, without a device copy of the result.
+ * FE_HOST_OUTPUT_AFTER: assembled into device staging, copied afterwards.
+ * The values are the same bit for bit in every mode.  Other host memory
+ * (pageable) takes the streamed or the after path.  chunks: the launches of a
+ * streamed assembly, 1..16, or 0 to choose by the output size (one per 48 MB
+ * of host output). */
+#define FE_HOST_OUTPUT_STREAMED 0
+#define FE_HOST_OUTPUT_IN_PLACE 1
+#define FE_HOST_OUTPUT_AFTER 2
+int fe_set_host_output(fe_handle h, int32_t mode, int32_t chunks);
 
 /* Element-level evaluation for a contiguous range of elements (0-based), the
  * direct counterparts of FiniteElasticity_FiniteElementResidualEvaluate /

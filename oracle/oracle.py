@@ -189,6 +189,7 @@ class EquationsSet:
 
     def __init__(self, mesh, nthreads=4):
         self.mesh = mesh
+        self.materials = np.asarray(mesh.materials, dtype=np.float64)
         self.prob = Problem(mesh)
         self.rp1, self.col1 = self.prob.pattern()
         self.ndofs = int(self.prob.ndofs)
@@ -205,6 +206,7 @@ class EquationsSet:
         import copy
         m = copy.copy(self.mesh)
         m.materials = np.asarray(materials, dtype=np.float64)
+        self.materials = m.materials
         sp = self.prob.surf_p
         self.prob = Problem(m)
         if sp is not None:

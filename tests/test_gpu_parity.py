@@ -8,6 +8,8 @@ of the terms, not by the entry.  The CSR pattern must match bit for bit.
 The FP32 block of the mixed path (tensor-core contraction) is checked at
 MIXED_UU_TOL relative to S.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -130,6 +132,53 @@ def test_mixed_outputs_in_pinned_pageable_and_device_memory(torch, order):
         es.jacobian_evaluate_mixed(x, hu, hc, hr)
         for a, b in zip((hu, hc, hr), ref):  # no synchronisation: the call has waited
             assert np.array_equal(a, b), (order, pinned)
+
+
+@pytest.mark.parametrize("case", ["box", "shuffled_elements", "element_pressure"])
+def test_streamed_host_outputs(torch, case):
+    """Host outputs delivered chunk by chunk while the remaining elements
+    assemble (fe_set_host_output streamed, 1..16 launches), written in place
+    or copied after the assembly: the same bits as device outputs, in
+    page-locked and pageable memory, for a call without the residual and with
+    one output in device memory, and for an element order unrelated to the
+    node numbering (rows then complete late; the last chunk copies them)."""
+    if case == "element_pressure":
+        m = M.regular_box(7, 6, 5, nxi_u=2, pressure="element", perturb=0.1, seed=3)
+    else:
+        m = M.regular_box(9, 7, 6, nxi_u=3, pressure="node", perturb=0.1, seed=3)
+        if case == "shuffled_elements":
+            perm = np.random.default_rng(5).permutation(m.ne)
+            m = dataclasses.replace(m, elem_u=np.ascontiguousarray(m.elem_u[perm]),
+                                    elem_p=np.ascontiguousarray(m.elem_p[perm]))
+    x = state(m)
+    es = FiniteElasticityEquationsSet(m)
+    xd = torch.from_numpy(x).cuda()
+    rd = torch.empty_like(xd)
+    ud, cd = es.jacobian_evaluate_mixed(xd, r=rd)
+    ref = [t.cpu().numpy() for t in (ud, cd, rd)]
+    l0 = es.launch_count()
+    es.set_host_output("streamed", 5)
+    es.jacobian_evaluate_mixed(x, *(np.empty_like(a) for a in ref))
+    assert es.launch_count() - l0 == 5
+    for mode, chunks in (("streamed", 0), ("streamed", 1), ("streamed", 3), ("streamed", 16),
+                         ("in_place", 0), ("after", 0)):
+        es.set_host_output(mode, chunks)
+        for pinned in (True, False):
+            bufs = [torch.full((es.nnz_uu,), float("nan"), dtype=torch.float32),
+                    torch.full((es.nnz_coupling,), float("nan"), dtype=torch.float64),
+                    torch.full((es.ndofs,), float("nan"), dtype=torch.float64)]
+            if pinned:
+                bufs = [b.pin_memory() for b in bufs]
+            hu, hc, hr = (b.numpy() for b in bufs)
+            es.jacobian_evaluate_mixed(x, hu, hc, hr)
+            for a, b in zip((hu, hc, hr), ref):  # no synchronisation: the call has waited
+                assert np.array_equal(a, b), (case, mode, chunks, pinned)
+        hu = np.full(es.nnz_uu, np.nan, dtype=np.float32)
+        cdev = torch.full((es.nnz_coupling,), float("nan"), dtype=torch.float64, device="cuda")
+        es.jacobian_evaluate_mixed(x, hu, cdev, None)
+        assert np.array_equal(hu, ref[0]) and np.array_equal(cdev.cpu().numpy(), ref[1]), (case, mode, chunks)
+    with pytest.raises(FEError):
+        es.set_host_output("streamed", 17)
 
 
 def test_deterministic(torch):

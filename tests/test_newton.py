@@ -69,8 +69,12 @@ def test_config1_uniaxial_exact_solution(oracle):
     pressure that makes the lateral faces traction-free."""
     m = cube_cfg1()
     lam = 1.1
-    x, reps = oracle_solve(oracle, m, N.uniaxial_symmetry_conditions(m, lam), 5, linear="dense")
+    es = oracle.EquationsSet(m)
+    s = N.LoadStepSolver(es, N.uniaxial_symmetry_conditions(m, lam), N.NewtonOptions(linear="dense"), device="cpu")
+    seen = []
+    x, reps = s.solve(torch.from_numpy(N.initial_state(m)), 5, progress=lambda i, r: seen.append((i, r)))
     assert len(reps) == 5 and all(r.converged for r in reps)
+    assert [i for i, _ in seen] == [1, 2, 3, 4, 5] and [r for _, r in seen] == reps
     for r in reps:
         assert r.iterations <= 5
         rn = r.residual_norms
@@ -127,6 +131,32 @@ def test_multigrid_preconditioned_gmres(oracle):
     sj = N.LoadStepSolver(es, bc, N.NewtonOptions(linear="gmres", max_iterations=1), device="cpu")
     _, rj = sj.solve(torch.from_numpy(N.initial_state(m)), 1)
     assert max(rm[0].linear_iterations) * 3 < rj[0].linear_iterations[0]
+
+
+def test_multigrid_vertex_coarse_operator(oracle):
+    """The first coarse operator by rediscretisation on the vertex mesh: the
+    vertex mesh carries the fine vertices' coordinates and the injected state
+    (nodal pressure included), and multigrid-preconditioned GMRES reaches the
+    same Newton iterates as with the Galerkin coarse operator, in a similar
+    number of Krylov iterations."""
+    if not _cpu_sparse_products():
+        pytest.skip("this PyTorch build has no CPU sparse CSR products")
+    from cm_gb300 import multigrid as MG
+    m = M.regular_box(4, 3, 2, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0), perturb=0.1, seed=5)
+    cm, inj = MG.vertex_mesh(m)
+    assert cm.nxi_u == 2 and cm.ne == m.ne and cm.grid_u == (5, 4, 3)
+    i, j, k = m.node_ijk()
+    vert = (i % 2 == 0) & (j % 2 == 0) & (k % 2 == 0)
+    assert np.array_equal(np.sort(inj[:cm.nu]), np.nonzero(vert)[0])
+    assert np.array_equal(cm.X, m.X[:, inj[:cm.nu]])
+    assert np.array_equal(inj[3 * cm.nu:], 3 * m.nu + np.arange(cm.n_pressure))
+    assert np.array_equal(m.pressure_node_u(), inj[:cm.nu])  # pressure nodes are the vertices, numbered alike
+    bc = N.clamped_stretch_shear_conditions(m, 1.05, 0.02)
+    xv, rv = oracle_solve(oracle, m, bc, 1, linear="mg", gmres_rtol=1e-8, mg_coarse="vertex")
+    xg, rg = oracle_solve(oracle, m, bc, 1, linear="mg", gmres_rtol=1e-8, mg_coarse="galerkin")
+    assert rv[0].converged and rg[0].converged and rv[0].iterations == rg[0].iterations
+    assert float((xv - xg).abs().max()) < 1e-9
+    assert max(rv[0].linear_iterations) <= 2 * max(rg[0].linear_iterations)
 
 
 def test_multigrid_prolongation_is_exact_for_linear_fields():
@@ -269,11 +299,12 @@ def test_gpu_gmres_path(cuda, oracle):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_gpu_multigrid_newton(cuda, oracle, precision):
+@pytest.mark.parametrize("coarse", ["vertex", "galerkin"])
+def test_gpu_multigrid_newton(cuda, oracle, precision, coarse):
     m = M.regular_box(4, 4, 4, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0), perturb=0.1, seed=1)
     bc = N.clamped_stretch_shear_conditions(m, 1.1, 0.05)
     xo, ro = oracle_solve(oracle, m, bc, 2, linear="dense")
-    xg, rg, _ = gpu_solve(m, bc, 2, linear="mg", precision=precision, gmres_rtol=1e-8)
+    xg, rg, _ = gpu_solve(m, bc, 2, linear="mg", precision=precision, gmres_rtol=1e-8, mg_coarse=coarse)
     assert all(r.converged for r in rg)
     assert all(max(r.linear_iterations) < 80 for r in rg)
     assert float((xg - xo).abs().max()) < 1e-9
