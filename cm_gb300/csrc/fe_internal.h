@@ -153,6 +153,10 @@ int launch_mixed(const HostSetup& s, const KParams& kp, int num_sms, void* strea
 // Elements per group of the fused kernel for this element type.
 int fused_group_size(const HostSetup& s);
 
+// Blocks of the fused kernel resident on the whole GPU at once (the groups
+// one wave of the launch takes); a negative cudaError_t on failure.
+int fused_wave(const HostSetup& s, int num_sms, bool double_float);
+
 // Launches the mixed-precision assembly kernel over all elements with its
 // output staged per element (so; fe_mixed.cu), in
 // one launch, without colour order.  Returns a cudaError_t value.

@@ -619,24 +619,27 @@ int ensure(void** buf, size_t bytes);
 // Group counters at the head of d_fuse: the most launches one fused assembly
 // is split into.
 constexpr int kFuseChunks = 64;
-// The most chunks a streamed assembly is split into.
+// The most chunks a streamed assembly is split into, and the most the
+// default plan uses.
 constexpr int kStreamChunks = 16;
+constexpr int kStreamAuto = 8;
 
 // The fused staged assembly (element records and row gathers in one kernel)
-// in `chunks` launches over consecutive ranges of element groups; when `done`
-// is given, done[c] is recorded on the stream after launch c.  The per-node
-// counts run on across the launches: a node's rows are gathered by the launch
-// that assembles the last element around it.
+// in launches over consecutive ranges of element groups, launch c taking
+// groups [bounds[c], bounds[c + 1]); when `done` is given, done[c] is
+// recorded on the stream after launch c.  The per-node counts run on across
+// the launches: a node's rows are gathered by the launch that assembles the
+// last element around it.
 int mixed_fused(fe_handle h, const KParams& kp, const cmfe::StageOut& so, bool double_float, cudaStream_t st,
-                int chunks, cudaEvent_t* done, int64_t* count) {
+                const std::vector<int64_t>& bounds, cudaEvent_t* done, int64_t* count) {
   const auto& s = h->hs;
   int rc;
+  const int chunks = (int)bounds.size() - 1;
+  if (chunks < 1 || chunks > kFuseChunks) return set_error(FE_ERR_INVALID_ARGUMENT, "fused launches: 1..64");
   const size_t counters = kFuseChunks + (size_t)s.nu + (size_t)s.npn;
   if ((rc = ensure((void**)&h->d_fuse, sizeof(int) * counters))) return rc;
   CUDA_TRY(cudaMemsetAsync(h->d_fuse, 0, sizeof(int) * counters, st));
   const int nb = s.bnd_ptr.empty() ? 0 : s.bnd_ptr[s.ncolours];
-  const int64_t groups = (s.ne + cmfe::fused_group_size(s) - 1) / cmfe::fused_group_size(s);
-  chunks = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)chunks, (int64_t)kFuseChunks, groups}));
   cmfe::FusedArgs fa;
   std::memset(&fa, 0, sizeof(fa));
   fa.u_inc_ptr = h->d_u_inc_ptr;
@@ -647,8 +650,8 @@ int mixed_fused(fe_handle h, const KParams& kp, const cmfe::StageOut& so, bool d
   fa.bmask = h->has_surfp && nb > 0 ? h->d_bnd_mask : nullptr;
   for (int c = 0; c < chunks; ++c) {
     fa.work = h->d_fuse + c;
-    fa.g0 = (int)(groups * c / chunks);
-    fa.g1 = (int)(groups * (c + 1) / chunks);
+    fa.g0 = (int)bounds[c];
+    fa.g1 = (int)bounds[c + 1];
     const int e = cmfe::launch_mixed_fused(s, kp, so, fa, h->num_sms, st, double_float);
     if (e != 0)
       return set_error(FE_ERR_CUDA, std::string("fused kernel launch: ") + cudaGetErrorString((cudaError_t)e));
@@ -657,6 +660,11 @@ int mixed_fused(fe_handle h, const KParams& kp, const cmfe::StageOut& so, bool d
   h->launches += chunks;
   if (count) *count += chunks;
   return FE_NO_ERROR;
+}
+
+int64_t fused_groups(const HostSetup& s) {
+  const int eg = cmfe::fused_group_size(s);
+  return (s.ne + eg - 1) / eg;
 }
 
 int ensure_records(fe_handle h) {
@@ -693,7 +701,7 @@ int mixed_staged(fe_handle h, const double* dx, float* du, double* dc, double* d
   if ((rc = ensure_records(h))) return rc;
   const KParams kp = staged_params(h, dx, du, dc, dr);
   const cmfe::StageOut so{h->d_st_uu, h->d_st_cp, h->d_st_r};
-  if (cmfe::fused_fits(s)) return mixed_fused(h, kp, so, double_float, st, 1, nullptr, count);
+  if (cmfe::fused_fits(s)) return mixed_fused(h, kp, so, double_float, st, {0, fused_groups(s)}, nullptr, count);
   const int nb = s.bnd_ptr.empty() ? 0 : s.bnd_ptr[s.ncolours];
   int e = cmfe::launch_mixed_staged(s, kp, so, h->num_sms, st, double_float);
   if (e != 0) return set_error(FE_ERR_CUDA, std::string("staged kernel launch: ") + cudaGetErrorString((cudaError_t)e));
@@ -722,13 +730,28 @@ int mixed_streamed(fe_handle h, const double* dx, float* du, double* dc, double*
   const auto& s = h->hs;
   int rc;
   if ((rc = ensure_records(h))) return rc;
-  const int64_t groups = (s.ne + cmfe::fused_group_size(s) - 1) / cmfe::fused_group_size(s);
-  const size_t host_bytes = (hu ? sizeof(float) * (size_t)s.nnz_uu : 0) +
-                            (hc ? sizeof(double) * (size_t)s.nnz_cp : 0) + (hr ? sizeof(double) * (size_t)s.ndofs : 0);
-  // chunks of about 48 MB of output: small enough that the last copy, which
-  // nothing overlaps, is short; few enough that each launch's tail is too
-  const int64_t want = h->stream_chunks > 0 ? h->stream_chunks : (int64_t)(host_bytes / (48u << 20)) + 1;
-  const int chunks = (int)std::max<int64_t>(1, std::min<int64_t>({want, (int64_t)kStreamChunks, groups}));
+  const int64_t groups = fused_groups(s);
+  const int wave = cmfe::fused_wave(s, h->num_sms, double_float);
+  if (wave <= 0)
+    return set_error(FE_ERR_CUDA, std::string("fused kernel occupancy: ") + cudaGetErrorString((cudaError_t)-wave));
+  // By default the launch boundaries fall on whole waves of the resident
+  // blocks, so that no launch but the last ends with part of the GPU idle:
+  // one wave first (the copies start early), then equal runs of waves, at
+  // most kStreamAuto launches (each launch adds seven copies to the copy
+  // stream).  An explicit count splits the groups evenly.
+  std::vector<int64_t> bounds{0};
+  const int64_t waves = (groups + wave - 1) / wave;
+  if (h->stream_chunks > 0) {
+    for (int c = 1; c <= h->stream_chunks; ++c) {
+      const int64_t g = groups * c / h->stream_chunks;
+      if (g > bounds.back()) bounds.push_back(g);
+    }
+  } else {
+    const int64_t run = std::max<int64_t>(1, (waves - 1 + kStreamAuto - 2) / (kStreamAuto - 1));
+    for (int64_t g = std::min<int64_t>(wave, groups); bounds.back() < groups; g = std::min<int64_t>(g + run * wave, groups))
+      bounds.push_back(g);
+  }
+  const int chunks = (int)bounds.size() - 1;
   if (!h->copy_stream) CUDA_TRY(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
   while ((int)h->chunk_events.size() < kStreamChunks + 1) {
     cudaEvent_t ev;
@@ -738,7 +761,7 @@ int mixed_streamed(fe_handle h, const double* dx, float* du, double* dc, double*
   const KParams kp = staged_params(h, dx, du, dc, dr);
   const cmfe::StageOut so{h->d_st_uu, h->d_st_cp, h->d_st_r};
   cudaEvent_t* ev = h->chunk_events.data();
-  if ((rc = mixed_fused(h, kp, so, double_float, st, chunks, ev, nullptr))) return rc;
+  if ((rc = mixed_fused(h, kp, so, double_float, st, bounds, ev, nullptr))) return rc;
   cudaStream_t cs = h->copy_stream;
   const int nu = s.nu, npn = s.npn, EG = cmfe::fused_group_size(s);
   auto copy_rows = [&](int64_t r0, int64_t r1) -> int {
@@ -751,12 +774,11 @@ int mixed_streamed(fe_handle h, const double* dx, float* du, double* dc, double*
       const int64_t a = s.cp_row_ptr[r0], b = s.cp_row_ptr[r1];
       if (b > a) CUDA_TRY(cudaMemcpyAsync(hc + a, dc + a, sizeof(double) * (b - a), cudaMemcpyDeviceToHost, cs));
     }
-    if (hr) CUDA_TRY(cudaMemcpyAsync(hr + r0, dr + r0, sizeof(double) * (r1 - r0), cudaMemcpyDeviceToHost, cs));
     return FE_NO_ERROR;
   };
   int a0 = 0, q0 = 0;
   for (int c = 0; c < chunks; ++c) {
-    const int64_t end = std::min<int64_t>(groups * (c + 1) / chunks * EG, s.ne);  // elements assembled
+    const int64_t end = std::min<int64_t>(bounds[c + 1] * EG, s.ne);  // elements assembled
     int a1 = nu, q1 = npn;
     if (c + 1 < chunks) {
       a1 = (int)(std::upper_bound(s.u_last_prefix.begin(), s.u_last_prefix.end(), (int32_t)(end - 1)) -
@@ -771,6 +793,11 @@ int mixed_streamed(fe_handle h, const double* dx, float* du, double* dc, double*
     if ((rc = copy_rows(3 * (int64_t)nu + q0, 3 * (int64_t)nu + q1))) return rc;
     a0 = a1;
     q0 = q1;
+  }
+  // the residual (one value per row: small) in one copy after the last launch
+  if (hr) {
+    CUDA_TRY(cudaStreamWaitEvent(cs, ev[chunks - 1], 0));
+    CUDA_TRY(cudaMemcpyAsync(hr, dr, sizeof(double) * (size_t)s.ndofs, cudaMemcpyDeviceToHost, cs));
   }
   CUDA_TRY(cudaEventRecord(ev[kStreamChunks], cs));
   CUDA_TRY(cudaStreamWaitEvent(st, ev[kStreamChunks], 0));

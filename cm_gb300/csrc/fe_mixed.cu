@@ -103,29 +103,40 @@ __global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB)
   }
 }
 
+// Resident blocks per SM of the fused kernel (its shared-memory attribute set
+// once per device first); 0 on error, with the error in *err.
 template <int N1, int PM, int SPLIT, class H>
-int launch_fused_t(const KParams& kp, const cmfe::StageOut& so, cmfe::FusedArgs fa, int gather_bytes, int num_sms,
-                   cudaStream_t st) {
+int fused_per_sm(cudaError_t* err) {
   using C = MixCfg<N1, PM>;
   static std::atomic<bool> attr[64];
   auto kern = fe_mixed_fused_kernel<N1, PM, SPLIT, H>;
   int dev = 0;
-  cudaError_t e0 = cudaGetDevice(&dev);
-  if (e0 != cudaSuccess) return (int)e0;
+  *err = cudaGetDevice(&dev);
+  if (*err != cudaSuccess) return 0;
   if (dev < 0 || dev >= 64 || !attr[dev].load()) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
-    if (e != cudaSuccess) return (int)e;
+    *err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+    if (*err != cudaSuccess) return 0;
     if (dev >= 0 && dev < 64) attr[dev].store(true);
   }
+  int per_sm = 0;
+  *err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::THREADS, C::SMEM);
+  if (*err != cudaSuccess) return 0;
+  return per_sm < 1 ? 1 : per_sm;
+}
+
+template <int N1, int PM, int SPLIT, class H>
+int launch_fused_t(const KParams& kp, const cmfe::StageOut& so, cmfe::FusedArgs fa, int gather_bytes, int num_sms,
+                   cudaStream_t st) {
+  using C = MixCfg<N1, PM>;
+  auto kern = fe_mixed_fused_kernel<N1, PM, SPLIT, H>;
   const int avail = C::O_READY - C::O_SCRATCH;
   fa.gbytes = gather_bytes;
   fa.gwarps = gather_bytes > 0 ? avail / gather_bytes : 0;
   if (fa.gwarps > C::THREADS / 32) fa.gwarps = C::THREADS / 32;
   if (fa.gwarps < 1) return (int)cudaErrorInvalidConfiguration;
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::THREADS, C::SMEM);
-  if (e != cudaSuccess) return (int)e;
-  per_sm = per_sm < 1 ? 1 : per_sm;
+  cudaError_t e;
+  const int per_sm = fused_per_sm<N1, PM, SPLIT, H>(&e);
+  if (!per_sm) return (int)e;
   const int all = (kp.count + C::EG - 1) / C::EG;
   if (fa.g1 > all) fa.g1 = all;
   if (fa.g0 < 0 || fa.g0 >= fa.g1) return (int)cudaSuccess;  // no groups in this launch
@@ -197,6 +208,19 @@ int launch_mixed(const HostSetup& s, const KParams& kp, int num_sms, void* strea
   cudaStream_t st = (cudaStream_t)stream;
   if (kp.count <= 0) return 0;
   return double_float ? launch_h<dd>(s, kp, num_sms, st) : launch_h<double>(s, kp, num_sms, st);
+}
+
+int fused_wave(const HostSetup& s, int num_sms, bool double_float) {
+  cudaError_t e;
+  int per_sm;
+  if (double_float)
+    per_sm = s.n1 == 2 ? (s.pmode ? fused_per_sm<2, 1, 3, dd>(&e) : fused_per_sm<2, 0, 3, dd>(&e))
+                       : (s.pmode ? fused_per_sm<3, 1, 3, dd>(&e) : fused_per_sm<3, 0, 3, dd>(&e));
+  else
+    per_sm = s.n1 == 2 ? (s.pmode ? fused_per_sm<2, 1, 3, double>(&e) : fused_per_sm<2, 0, 3, double>(&e))
+                       : (s.pmode ? fused_per_sm<3, 1, 3, double>(&e) : fused_per_sm<3, 0, 3, double>(&e));
+  if (!per_sm) return -(int)e;
+  return per_sm * (num_sms > 0 ? num_sms : 1);
 }
 
 int fused_group_size(const HostSetup& s) {

@@ -245,7 +245,8 @@ class FiniteElasticityEquationsSet:
     def set_host_output(self, mode, chunks=0):
         """fe_set_host_output: how jacobian_evaluate_mixed delivers outputs in
         host memory -- "streamed" (the default: rows copied to the host chunk
-        by chunk while the rest assembles; `chunks` launches, 0 = by size),
+        by chunk while the rest assembles; `chunks` equal launches, or 0 for
+        launches on whole waves of the kernel's resident blocks),
         "in_place" (page-locked outputs written by the row gather over the
         host link) or "after" (one copy after the assembly).  The values are
         identical in every mode."""

@@ -214,15 +214,18 @@ int fe_set_assembly_order(fe_handle h, int32_t order);
  * up to 16 launches over consecutive ranges of elements; after each, the rows
  * whose elements are all assembled (for a mesh numbered like the elements,
  * the leading rows of each row block) are copied to the host on a second
- * stream while the next launches run.  Device staging for the outputs.
+ * stream while the next launches run; the residual follows in one copy.
+ * Device staging for the outputs.  By default at most 8 launches, ending on
+ * whole waves of the kernel's resident blocks: one wave first, then equal
+ * runs of waves.
  * FE_HOST_OUTPUT_IN_PLACE (staged order): outputs in page-locked host memory
  * (cudaHostAlloc / cudaHostRegister) are written in place by the row gather
  * over the host link, without a device copy of the result.
  * FE_HOST_OUTPUT_AFTER: assembled into device staging, copied afterwards.
  * The values are the same bit for bit in every mode.  Other host memory
  * (pageable) takes the streamed or the after path.  chunks: the launches of a
- * streamed assembly, 1..16, or 0 to choose by the output size (one per 48 MB
- * of host output). */
+ * streamed assembly, 1..16 of equal element counts, or 0 for the wave plan
+ * above. */
 #define FE_HOST_OUTPUT_STREAMED 0
 #define FE_HOST_OUTPUT_IN_PLACE 1
 #define FE_HOST_OUTPUT_AFTER 2
