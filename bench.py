@@ -491,6 +491,14 @@ def our_arm(args):
         else:
             out["loadstep"] = loadstep_leg(dev, n=args.loadstep_size, n_train=args.loadstep_train,
                                            n_test=args.loadstep_test, increments=args.loadstep_increments)
+    if world == 1 and args.config == "cfg2" and args.extra and args.loadstep:
+        # the configuration's own loading: 10 increments to stretch 1.2 / shear 0.1 on the same mesh,
+        # plain FP64 against mixed + Eisenstat-Walker (about two minutes)
+        torch.cuda.empty_cache()
+        try:
+            out["config2_loading"] = config2_loading_leg(dev, arms_wanted=["plain_fp64", "mixed_ew"])
+        except Exception as e:  # the assembly line above stands on its own
+            out["config2_loading"] = {"error": "%s: %s" % (type(e).__name__, e)}
     print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
@@ -1046,7 +1054,8 @@ def main():
     ap.add_argument("--no-loadstep", dest="loadstep", action="store_false",
                     help="skip the Newton load-step comparison (plain FP64 vs mixed + learned warm start)")
     ap.add_argument("--no-extra", dest="extra", action="store_false",
-                    help="skip the batched legs (256 box meshes, 32 slab variants) of the default configuration")
+                    help="skip the extra legs of the default configuration (256 box meshes, 32 slab variants, "
+                         "the 10-increment loading)")
     ap.add_argument("--config2-arms", default="",
                     help="comma-separated arms of --config2-loading (plain_fp64, mixed, mixed_ew; default all)")
     ap.add_argument("--config2-loading", action="store_true",

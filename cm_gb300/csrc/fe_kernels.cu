@@ -622,7 +622,7 @@ constexpr int kFuseChunks = 64;
 // The most chunks a streamed assembly is split into, and the most the
 // default plan uses.
 constexpr int kStreamChunks = 16;
-constexpr int kStreamAuto = 8;
+constexpr int kStreamAuto = 12;
 
 // The fused staged assembly (element records and row gathers in one kernel)
 // in launches over consecutive ranges of element groups, launch c taking
@@ -736,9 +736,10 @@ int mixed_streamed(fe_handle h, const double* dx, float* du, double* dc, double*
     return set_error(FE_ERR_CUDA, std::string("fused kernel occupancy: ") + cudaGetErrorString((cudaError_t)-wave));
   // By default the launch boundaries fall on whole waves of the resident
   // blocks, so that no launch but the last ends with part of the GPU idle:
-  // one wave first (the copies start early), then equal runs of waves, at
-  // most kStreamAuto launches (each launch adds seven copies to the copy
-  // stream).  An explicit count splits the groups evenly.
+  // equal runs of waves, at most kStreamAuto launches (each launch adds seven
+  // copies to the copy stream; smaller first launches do not start the copies
+  // sooner, since a node's rows complete only with the next layer of
+  // elements).  An explicit count splits the groups evenly.
   std::vector<int64_t> bounds{0};
   const int64_t waves = (groups + wave - 1) / wave;
   if (h->stream_chunks > 0) {
@@ -747,8 +748,9 @@ int mixed_streamed(fe_handle h, const double* dx, float* du, double* dc, double*
       if (g > bounds.back()) bounds.push_back(g);
     }
   } else {
-    const int64_t run = std::max<int64_t>(1, (waves - 1 + kStreamAuto - 2) / (kStreamAuto - 1));
-    for (int64_t g = std::min<int64_t>(wave, groups); bounds.back() < groups; g = std::min<int64_t>(g + run * wave, groups))
+    const int64_t run = std::max<int64_t>(1, (waves + kStreamAuto - 1) / kStreamAuto);
+    for (int64_t g = std::min<int64_t>(run * wave, groups); bounds.back() < groups;
+         g = std::min<int64_t>(g + run * wave, groups))
       bounds.push_back(g);
   }
   const int chunks = (int)bounds.size() - 1;

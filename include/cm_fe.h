@@ -215,9 +215,8 @@ int fe_set_assembly_order(fe_handle h, int32_t order);
  * whose elements are all assembled (for a mesh numbered like the elements,
  * the leading rows of each row block) are copied to the host on a second
  * stream while the next launches run; the residual follows in one copy.
- * Device staging for the outputs.  By default at most 8 launches, ending on
- * whole waves of the kernel's resident blocks: one wave first, then equal
- * runs of waves.
+ * Device staging for the outputs.  By default at most 12 launches of equal
+ * runs of whole waves of the kernel's resident blocks.
  * FE_HOST_OUTPUT_IN_PLACE (staged order): outputs in page-locked host memory
  * (cudaHostAlloc / cudaHostRegister) are written in place by the row gather
  * over the host link, without a device copy of the result.
