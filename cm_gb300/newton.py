@@ -48,6 +48,8 @@ class NewtonOptions:
     forcing: str = "constant"    # "constant" (gmres_rtol) or "ew" (Eisenstat-Walker choice 2)
     mg_coarse: str = "vertex"    # first coarse operator of a triquadratic mesh: "vertex" (the trilinear
     #                              vertex mesh assembled at the injected state) or "galerkin" (P^T A P)
+    mg_graph: bool = True        # record the whole preconditioner application (V-cycle, pressure-mass
+    #                              solve, coupling SpMV) in one CUDA graph per Newton iteration
 
 
 @dataclass
@@ -156,6 +158,33 @@ class FreeDofSystem:
         return A, B
 
 
+def _graphed(f, n, device):
+    """f (a function of one FP64 vector of length n that launches only device
+    work) recorded in a CUDA graph with a static input and output; f itself
+    if the capture is refused."""
+    w_in = torch.zeros(n, dtype=torch.float64, device=device)
+    cur = torch.cuda.current_stream(device)
+    side = torch.cuda.Stream(device)
+    side.wait_stream(cur)
+    with torch.cuda.stream(side):
+        for _ in range(2):  # warm-up outside the capture (library handles, workspaces)
+            f(w_in)
+    cur.wait_stream(side)
+    g = torch.cuda.CUDAGraph()
+    try:
+        with torch.cuda.graph(g):
+            out = f(w_in)
+    except RuntimeError:
+        torch.cuda.synchronize(device)
+        return f
+
+    def replay(w):
+        w_in.copy_(w)
+        g.replay()
+        return out.clone()
+    return replay
+
+
 def _gmres(A, b, M, rtol, restart, max_it, check_every=6):
     """Right-preconditioned restarted GMRES (FP64); M(v) applies the preconditioner.
 
@@ -251,7 +280,8 @@ class LoadStepSolver:
             from .multigrid import BoxMultigrid, MassSolver, pressure_mass_matrix
             m = es.mesh
             self.mg = BoxMultigrid(m.grid_u, m.nxi_u, self.free_mask[:3 * m.nu], self.device,
-                                   torch.float32 if self.opt.precision == "mixed" else torch.float64)
+                                   torch.float32 if self.opt.precision == "mixed" else torch.float64,
+                                   use_graph=not self.opt.mg_graph)
             self.coarse = None
             if self.opt.mg_coarse == "vertex" and m.nxi_u == 3 and len(self.mg.free) > 1:
                 from .multigrid import VertexOperator, vertex_mesh
@@ -358,6 +388,8 @@ class LoadStepSolver:
             zu = self.mg.vcycle(w[:nfu].to(mg_dtype)).to(torch.float64)
             zp = self.mass_solver.solve(B @ zu - w[nfu:]) / scale
             return torch.cat([zu, zp])
+        if self.device.type == "cuda" and self.opt.mg_graph:
+            return _graphed(apply, S.nf, self.device)
         return apply
 
     def linear_solve(self, A, b, rtol=None):
