@@ -161,7 +161,8 @@ class FreeDofSystem:
 def _graphed(f, n, device):
     """f (a function of one FP64 vector of length n that launches only device
     work) recorded in a CUDA graph with a static input and output; f itself
-    if the capture is refused."""
+    if the capture is refused.  The returned function holds f, and so every
+    tensor f reads: the graph replays their device addresses."""
     w_in = torch.zeros(n, dtype=torch.float64, device=device)
     cur = torch.cuda.current_stream(device)
     side = torch.cuda.Stream(device)
@@ -178,7 +179,7 @@ def _graphed(f, n, device):
         torch.cuda.synchronize(device)
         return f
 
-    def replay(w):
+    def replay(w, _source=f):
         w_in.copy_(w)
         g.replay()
         return out.clone()

@@ -221,8 +221,10 @@ int fe_set_assembly_order(fe_handle h, int32_t order);
  * (cudaHostAlloc / cudaHostRegister) are written in place by the row gather
  * over the host link, without a device copy of the result.
  * FE_HOST_OUTPUT_AFTER: assembled into device staging, copied afterwards.
- * The values are the same bit for bit in every mode.  Other host memory
- * (pageable) takes the streamed or the after path.  chunks: the launches of a
+ * The values are the same bit for bit in every mode.  Where the streamed or
+ * in-place mode does not apply (the coloured order; for streaming, a mesh
+ * whose row neighbourhoods exceed the fused kernel's scratch; for in place,
+ * pageable memory) the call copies after the assembly.  chunks: the launches of a
  * streamed assembly, 1..16 of equal element counts, or 0 for the wave plan
  * above. */
 #define FE_HOST_OUTPUT_STREAMED 0
