@@ -854,7 +854,11 @@ def config4_study(dev, n=16, n_train=2048, n_test=256, n_timed=32, increments=10
     train = W.sample_parameters(n_train, seed=21)
     test = W.sample_parameters(n_test, seed=22)
     t0 = time.perf_counter()
-    states, it_train = W.generate_solves(learned, train, increments, continuation=True, steps=2)
+    def progress(done, i, newton, sec):
+        if sec > 10.0 or done % 64 == 0:
+            print("config4: training solve %d/%d (row %d): %d Newton, %.1f s; %.1f s so far"
+                  % (done, n_train, i, newton, sec, time.perf_counter() - t0), file=sys.stderr, flush=True)
+    states, it_train = W.generate_solves(learned, train, increments, continuation=True, steps=2, progress=progress)
     t_data = time.perf_counter() - t0
     print("config4: %d training solves in %.1f s" % (n_train, t_data), file=sys.stderr, flush=True)
     ws = W.LearnedWarmStart(learned.n_pressure, modes=min(modes, n_train - 1), seed=0, device=dev)

@@ -334,7 +334,7 @@ def _interpolate_parameters(a, b, t):
                      a[2] * (b[2] / a[2]) ** t, a[3] * (b[3] / a[3]) ** t])
 
 
-def generate_solves(problem, params, increments, continuation=False, steps=1):
+def generate_solves(problem, params, increments, continuation=False, steps=1, progress=None):
     """Converged free-dof states for every parameter row.
 
     Without continuation every row is solved by the plain method (reference
@@ -344,7 +344,9 @@ def generate_solves(problem, params, increments, continuation=False, steps=1):
     full-load Newton solves at parameters interpolated between the two (the
     plain method where one of them does not converge); the converged states
     are the same (||r||_2 <= atol), only cheaper to reach.  Returns (states in
-    the order of params, Newton iterations per row)."""
+    the order of params, Newton iterations per row).  progress (optional) is
+    called after every row with (rows done, row index, Newton iterations of
+    the row, seconds of the row)."""
     n = len(params)
     order = list(range(n))
     if continuation and n > 1:
@@ -363,7 +365,8 @@ def generate_solves(problem, params, increments, continuation=False, steps=1):
     iters = np.zeros(n, dtype=np.int64)
     prev = None
     prev_p = None
-    for i in order:
+    for done, i in enumerate(order, start=1):
+        t_row = time.perf_counter()
         p = params[i]
         if prev is not None and steps > 1 and hasattr(problem, "newton_from_state"):
             reps, st, ok = [], prev, True
@@ -387,6 +390,8 @@ def generate_solves(problem, params, increments, continuation=False, steps=1):
         iters[i] = sum(r.iterations for r in reps)
         prev = states[i] if continuation else None
         prev_p = p
+        if progress is not None:
+            progress(done, i, int(iters[i]), time.perf_counter() - t_row)
     return torch.stack(states), iters
 
 
