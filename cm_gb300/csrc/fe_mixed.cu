@@ -57,13 +57,12 @@ __global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB)
   const int* s_node = reinterpret_cast<const int*>(sm + C::O_NODE);
   int* ready = reinterpret_cast<int*>(sm + C::O_READY);
   unsigned char* scratch = sm + C::O_SCRATCH;
-  if (tid == 0) s_grp = F.g0 + atomicAdd(F.work, 1);
-  __syncthreads();
   for (;;) {
+    if (tid == 0) s_grp = F.g0 + atomicAdd(F.work, 1);
+    __syncthreads();
     const int grp = s_grp;
     if (grp >= ngroups) break;
-    // every thread has read s_grp and passed a barrier since the last shared-memory store
-    mix_group<N1, PM, EG, SPLIT, H, 1, false>(P, nullptr, P.count, grp, p4_first, sm, &so);
+    mix_group<N1, PM, EG, SPLIT, H, 1>(P, nullptr, P.count, grp, p4_first, sm, &so);
     const int nvalid = min(EG, P.count - grp * EG);
     __syncthreads();  // the group's records are complete within the CTA; the scratch is free
     if (F.bmask) {
@@ -90,8 +89,6 @@ __global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB)
     }
     __syncthreads();
     const int nready = s_nready;
-    // the next group, taken while the gathers run; read after the closing barrier
-    if (tid == 0) s_grp = F.g0 + atomicAdd(F.work, 1);
     if (warp < F.gwarps) {
       unsigned char* mine = scratch + (size_t)warp * F.gbytes;
       for (int j = warp; j < nready; j += F.gwarps) {
@@ -102,7 +99,7 @@ __global__ void __launch_bounds__(256, MixCfg<N1, PM>::MINB)
           gather_pnode<NPE, NPP, true>(P, so, F.p_inc_ptr, F.p_inc, id - P.nu, mine, lane);
       }
     }
-    __syncthreads();  // the next group reuses the scratch and the ready list, and reads s_grp
+    __syncthreads();  // the next group reuses the scratch and the ready list
   }
 }
 

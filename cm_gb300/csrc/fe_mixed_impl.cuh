@@ -330,10 +330,8 @@ __device__ __forceinline__ int elem_at(const KParams& P, const int32_t* elems, i
 // (P3) and tensor-core (P4) stages.  OUT = 0 adds the element's entries into
 // the CSR values and the residual (first contributor in colour order stores,
 // later ones add); OUT = 1 stores them into the element's staging records
-// (*SO), which the row gather sums afterwards.  LEAD = false leaves out the
-// opening barrier, for callers that have just passed one with no shared
-// memory written since.
-template <int N1, int PM, int EG_, int SPLIT, class H, int OUT = 0, bool LEAD = true>
+// (*SO), which the row gather sums afterwards.
+template <int N1, int PM, int EG_, int SPLIT, class H, int OUT = 0>
 __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems, int count, int grp, bool p4_first,
                                           unsigned char* sm, const cmfe::StageOut* SO = nullptr) {
   using C = MixCfg<N1, PM, EG_>;
@@ -358,7 +356,7 @@ __device__ __forceinline__ void mix_group(const KParams& P, const int32_t* elems
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nu = P.nu;
   const int nvalid = min(EG, count - grp * EG);
-  if constexpr (LEAD) __syncthreads();
+  __syncthreads();
   // ---- P0: element nodes and table ids
   for (int i = tid; i < EG * (NR + 1); i += C::THREADS) {
     const int el = i / (NR + 1), r = i % (NR + 1);
