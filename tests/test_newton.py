@@ -159,6 +159,31 @@ def test_multigrid_vertex_coarse_operator(oracle):
     assert max(rv[0].linear_iterations) <= 2 * max(rg[0].linear_iterations)
 
 
+@pytest.mark.parametrize("kind", ["element_pressure", "guccione_fibres"])
+def test_vertex_mesh_carries_the_fine_data(kind):
+    """vertex_mesh for element-based pressure (one pressure dof per element,
+    injected element by element) and for a Guccione slab (fibre angles and
+    per-law materials taken at the vertices)."""
+    from cm_gb300 import multigrid as MG
+    if kind == "element_pressure":
+        m = M.regular_box(3, 2, 2, nxi_u=3, pressure="element", law=M.MR, materials=(1.0, 4.0), perturb=0.1, seed=2)
+    else:
+        m = M.guccione_slab(4, 3, 2, seed=1)
+    cm, inj = MG.vertex_mesh(m)
+    assert cm.p_mode == m.p_mode and cm.law == m.law and np.array_equal(cm.materials, m.materials)
+    assert cm.ne == m.ne and cm.ndofs == len(inj)
+    vid = inj[:cm.nu]
+    assert np.array_equal(cm.X, m.X[:, vid])
+    if m.fibre is not None:
+        assert np.array_equal(cm.fibre, m.fibre[:, vid])
+    # the corner nodes of every fine element are the coarse element's nodes, in the same order
+    corners = [a * 2 + b * 2 * 3 + c * 2 * 9 for c in (0, 1) for b in (0, 1) for a in (0, 1)]
+    assert np.array_equal(vid[cm.elem_u], m.elem_u[:, corners])
+    x = M.deformed_state(m, stretch=1.05, shear=0.02, noise=0.01, pressure=-0.5, seed=3)
+    xc = x[inj]
+    assert np.array_equal(xc[3 * cm.nu:], x[3 * m.nu:3 * m.nu + cm.n_pressure])
+
+
 def test_multigrid_prolongation_is_exact_for_linear_fields():
     """The tensor-product prolongations reproduce linear fields on every level
     (Q1 functions are in the Q2 space, and coarse Q1 in fine Q1)."""
