@@ -231,7 +231,7 @@ class BoxMultigrid:
 
     @staticmethod
     def _diag(A):
-        crow, col, val = A.crow_indices(), A.col_indices(), A.values()
+        crow, col, val = A.crow_indices().long(), A.col_indices().long(), A.values()
         rows = torch.repeat_interleave(torch.arange(A.shape[0], device=val.device), crow[1:] - crow[:-1])
         d = torch.zeros(A.shape[0], dtype=val.dtype, device=val.device)
         m = rows == col

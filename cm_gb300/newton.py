@@ -50,6 +50,8 @@ class NewtonOptions:
     #                              vertex mesh assembled at the injected state) or "galerkin" (P^T A P)
     mg_graph: bool = True        # record the whole preconditioner application (V-cycle, pressure-mass
     #                              solve, coupling SpMV) in one CUDA graph per Newton iteration
+    csr_index: str = "int64"     # index type of the free-dof CSR operators ("int32" reads 4 bytes
+    #                              fewer per entry in every SpMV of the Krylov operator and the fine level)
 
 
 @dataclass
@@ -114,7 +116,7 @@ class PressureIncrements:
 class FreeDofSystem:
     """Index maps from the full CSR pattern to the free-dof submatrix."""
 
-    def __init__(self, es, free_mask, device):
+    def __init__(self, es, free_mask, device, index_dtype=torch.int64):
         rp, col = es.csr_pattern(base=0)
         n = es.ndofs
         rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(rp))
@@ -126,8 +128,11 @@ class FreeDofSystem:
         r = new_index[rows[keep]]
         c = new_index[col[keep]]
         counts = np.bincount(r, minlength=self.nf)
-        self.crow = torch.from_numpy(np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)).to(device)
-        self.col = torch.from_numpy(c.astype(np.int64)).to(device)
+        if index_dtype == torch.int32 and int(keep.sum()) >= 2 ** 31:
+            index_dtype = torch.int64
+        ix = np.int32 if index_dtype == torch.int32 else np.int64
+        self.crow = torch.from_numpy(np.concatenate([[0], np.cumsum(counts)]).astype(ix)).to(device)
+        self.col = torch.from_numpy(c.astype(ix)).to(device)
         self.row = torch.from_numpy(r.astype(np.int64)).to(device)
         self.free = torch.from_numpy(np.nonzero(free_mask)[0]).to(device)
         self.is_p = torch.from_numpy(np.nonzero(free_mask)[0] >= 3 * es.mesh.nu).to(device)
@@ -140,12 +145,13 @@ class FreeDofSystem:
         am = (r < nfu) & (c < nfu)
         bm = (r >= nfu) & (c < nfu)
         self.a_sel = torch.from_numpy(np.nonzero(am)[0]).to(device)
-        self.a_crow = torch.from_numpy(np.concatenate([[0], np.cumsum(np.bincount(r[am], minlength=nfu))])).to(device)
-        self.a_col = torch.from_numpy(c[am].astype(np.int64)).to(device)
+        self.a_crow = torch.from_numpy(
+            np.concatenate([[0], np.cumsum(np.bincount(r[am], minlength=nfu))]).astype(ix)).to(device)
+        self.a_col = torch.from_numpy(c[am].astype(ix)).to(device)
         self.b_sel = torch.from_numpy(np.nonzero(bm)[0]).to(device)
         self.b_crow = torch.from_numpy(
-            np.concatenate([[0], np.cumsum(np.bincount(r[bm] - nfu, minlength=self.nfp))])).to(device)
-        self.b_col = torch.from_numpy(c[bm].astype(np.int64)).to(device)
+            np.concatenate([[0], np.cumsum(np.bincount(r[bm] - nfu, minlength=self.nfp))]).astype(ix)).to(device)
+        self.b_col = torch.from_numpy(c[bm].astype(ix)).to(device)
 
     def matrix(self, vals_full):
         v = vals_full[self.sel]
@@ -268,7 +274,8 @@ class LoadStepSolver:
         self.opt = options or NewtonOptions()
         self.device = torch.device(device)
         self.free_mask = bc.free_mask()
-        self.sys = FreeDofSystem(es, self.free_mask, self.device)
+        self.sys = FreeDofSystem(es, self.free_mask, self.device,
+                                 torch.int32 if self.opt.csr_index == "int32" else torch.int64)
         self.bc_dofs = torch.from_numpy(bc.dofs).to(self.device)
         if self.opt.precision == "mixed":
             es.set_high_precision(self.opt.high_precision)
@@ -379,8 +386,9 @@ class LoadStepSolver:
         dA = self.mg.dinv[0].to(torch.float64)
         sd = torch.zeros(S.nfp, dtype=torch.float64, device=self.device)
         bv = B.values()
-        brow = torch.repeat_interleave(torch.arange(S.nfp, device=self.device), B.crow_indices()[1:] - B.crow_indices()[:-1])
-        sd.index_add_(0, brow, bv * bv * dA[B.col_indices()])
+        bcrow = B.crow_indices().long()
+        brow = torch.repeat_interleave(torch.arange(S.nfp, device=self.device), bcrow[1:] - bcrow[:-1])
+        sd.index_add_(0, brow, bv * bv * dA[B.col_indices().long()])
         scale = float(torch.median(sd / self.mass_p))
         nfu = S.nfu
         self.setup_seconds += time.perf_counter() - t0

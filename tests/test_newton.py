@@ -335,6 +335,21 @@ def test_gpu_multigrid_newton(cuda, oracle, precision, coarse):
     assert float((xg - xo).abs().max()) < 1e-9
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,coarse", [("mixed", "vertex"), ("fp64", "galerkin")])
+def test_gpu_csr_int32_matches_int64(cuda, precision, coarse):
+    """32-bit CSR indices for the Krylov operator and the multigrid's fine
+    level: the same Newton iterates as with 64-bit indices."""
+    m = M.regular_box(4, 4, 4, nxi_u=3, pressure="node", law=M.MR, materials=(2.0, 6.0), perturb=0.1, seed=1)
+    bc = N.clamped_stretch_shear_conditions(m, 1.1, 0.05)
+    opt = dict(linear="mg", precision=precision, gmres_rtol=1e-8, mg_coarse=coarse)
+    x64, r64, _ = gpu_solve(m, bc, 2, **opt)
+    x32, r32, es = gpu_solve(m, bc, 2, csr_index="int32", **opt)
+    assert all(r.converged for r in r32)
+    assert [r.iterations for r in r32] == [r.iterations for r in r64]
+    assert float((x32 - x64).abs().max()) < 1e-9
+
+
 def test_pressure_increment_rule():
     # increment 1: FULL/N; then NEW = CUR + (CUR - PREV): a linear ramp to FULL
     full = np.array([[0.0, 2.0], [1.0, -3.0]])
