@@ -760,7 +760,7 @@ def config2_loading_leg(dev, increments=10, stretch=1.2, shear=0.1, arms_wanted=
     relative tolerance 1e-5, the reference default), the mixed Jacobian with
     the same tolerance, and the mixed Jacobian with Eisenstat-Walker forcing.
     The linear solver is GMRES with the multigrid block preconditioner in all
-    three."""
+    three, with 32-bit CSR indices."""
     import torch
 
     from cm_gb300 import FiniteElasticityEquationsSet
@@ -768,9 +768,9 @@ def config2_loading_leg(dev, increments=10, stretch=1.2, shear=0.1, arms_wanted=
     m, _, _ = config_mesh("cfg2")
     es = FiniteElasticityEquationsSet(m)
     bc = N.clamped_stretch_shear_conditions(m, stretch, shear)
-    arms = {"plain_fp64": N.NewtonOptions(linear="mg"),
-            "mixed": N.NewtonOptions(linear="mg", precision="mixed"),
-            "mixed_ew": N.NewtonOptions(linear="mg", precision="mixed", forcing="ew")}
+    arms = {"plain_fp64": N.NewtonOptions(linear="mg", csr_index="int32"),
+            "mixed": N.NewtonOptions(linear="mg", precision="mixed", csr_index="int32"),
+            "mixed_ew": N.NewtonOptions(linear="mg", precision="mixed", forcing="ew", csr_index="int32")}
     if arms_wanted:
         arms = {k: v for k, v in arms.items() if k in arms_wanted}
     out, xs = {}, {}
