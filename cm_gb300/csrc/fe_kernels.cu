@@ -500,7 +500,7 @@ struct fe_equations_set {
   double *d_st_cp = nullptr, *d_st_r = nullptr;
   int* d_fuse = nullptr;  // fused staged assembly: [0, kFuseChunks) group counters, then per-row-node counts
   int host_output = FE_HOST_OUTPUT_STREAMED;
-  int stream_chunks = 0;  // launches of a streamed assembly; 0: by the output size
+  int stream_chunks = 0;  // launches of a streamed assembly; 0: equal runs of whole waves
   // streamed host outputs: the copy stream and one event per chunk (+ the last copy)
   cudaStream_t copy_stream = nullptr;
   std::vector<cudaEvent_t> chunk_events;

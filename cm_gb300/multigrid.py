@@ -118,7 +118,10 @@ class VertexOperator:
     rediscretisation: the free displacement block of the Jacobian of
     `vertex_mesh(mesh)`, assembled by `coarse_es` (an equations set of that
     mesh) at the state injected from the fine one.  free_c is the mask of
-    free coarse displacement dofs (the multigrid's level-1 mask)."""
+    free coarse displacement dofs (the multigrid's level-1 mask).  A
+    surface-pressure load of the fine set is not carried over: its follower
+    stiffness is left out of this preconditioning operator, not of the
+    Newton system."""
 
     def __init__(self, mesh, coarse_es, free_c, device):
         self.es = coarse_es
