@@ -6,12 +6,11 @@ The reference writes its fields with FIELD_IO_NODES_EXPORT / FIELD_IO_ELEMENTS_E
 interpolation labels "l.Lagrange" / "q.Lagrange" and ", no modify, standard
 node based." :300-375, "coordinate, rectangular cartesian" :593, "#Nodes" /
 "#Fields" :641-647, " Node:" :1029, " Element: e 0 0" :814, "Nodes:" :833).
-This module writes the same layout for the fields of one equations set, so a
+This module writes the same files for the fields of one equations set, so a
 converged state can be compared with, or loaded next to, output of the
-reference: the undeformed geometry, the deformed geometry z (the dependent
-field's displacement components) and the hydrostatic pressure (nodal on the
-element corners, or element-constant).  Lagrange bases carry no derivatives
-and no scale factors.
+reference: the geometric field and the dependent field (deformed position and
+hydrostatic pressure, nodal on the element corners or element-constant).
+Both files are byte-identical to the reference writer's for the same state.
 """
 from __future__ import annotations
 
@@ -93,41 +92,79 @@ def write_exnode(path, mesh: Mesh, x, group="Region", geometry="Geometry", depen
         f.write("\n".join(lines) + "\n")
 
 
+def _element_bases(mesh: Mesh):
+    """The element components in field order (geometric x, y, z; dependent
+    1-4) as (field label, component label, basis key or None for an
+    element-constant component) and the bases by key: (per-xi label, local
+    u-node positions of the basis' nodes within the element)."""
+    n1 = mesh.nxi_u
+    bases = {"u": (_basis_label(n1), list(range(n1 ** 3)))}
+    comps = [("G", c, "u") for c in ("x", "y", "z")] + [("D", str(c), "u") for c in (1, 2, 3)]
+    if mesh.p_mode == 1:
+        corners = [(a * (n1 - 1)) + (b * (n1 - 1)) * n1 + (c * (n1 - 1)) * n1 * n1
+                   for c in (0, 1) for b in (0, 1) for a in (0, 1)]
+        bases["p"] = (_basis_label(2), corners)
+        comps.append(("D", "4", "p"))
+    else:
+        comps.append(("D", "4", None))
+    return comps, bases
+
+
 def write_exelem(path, mesh: Mesh, x=None, group="Region"):
-    """Element topology with the node-based interpolation of the two
-    geometric fields; element-constant pressure (when x is given and the
-    pressure is element based) as a constant, grid-based field."""
-    npe = mesh.nxi_u ** 3
-    label = _basis_label(mesh.nxi_u)
-    names = [("Geometry", "coordinate, rectangular cartesian"), ("DeformedGeometry", "field, rectangular cartesian")]
-    lines = [" Group name: %s" % group, " Shape.  Dimension=3", " #Scale factor sets= 0",
-             " #Nodes=           %d" % npe, " #Fields=%d" % len(names)]
-    for i, (name, kind) in enumerate(names, start=1):
-        lines.append(" %d) %s, %s, #Components=3" % (i, name, kind))
-        for c in ("x", "y", "z"):
-            lines.append("   %s.  %s, no modify, standard node based." % (c, label))
-            lines.append("     #Nodes= %d" % npe)
-            for a in range(npe):
-                lines.append("     %d.  #Values=1" % (a + 1))
-                lines.append("      Value indices:     1")
-                lines.append("      Scale factor indices:   0")
+    """Element file of the two fields, in the layout the reference's element
+    export writes (FIELD_IO_EXPORT_ELEMENTS_INTO_LOCAL_FILE and its header,
+    field_IO_routines.f90:2519-3853, through src/FieldExport.c): every element
+    of a mesh shares one header, written before the first element; one
+    scale-factor set per distinct basis (the default arithmetic-mean scaling:
+    unit factors for Lagrange bases), numbered in component order, the first
+    index of a later set being the reference's sum of the set sizes up to and
+    including it, minus one; per node-based component its nodes as positions in
+    the element's node list (the u basis), per element-constant component a
+    grid-based line; per element its number, the element-constant values
+    (element-based pressure from x), the u nodes and the scale factors of
+    every set."""
+    comps, bases = _element_bases(mesh)
+    keys = []
+    for _, _, k in comps:
+        if k is not None and k not in keys:
+            keys.append(k)
+    size = {k: len(bases[k][1]) for k in keys}
+    lines = [" Group name: %s" % group, " Shape.  Dimension=3", " #Scale factor sets= %d" % len(keys)]
+    lines += [" %s, #Scale factors=%d" % (bases[k][0], size[k]) for k in keys]
+    lines += [" #Nodes=           %d" % len(bases["u"][1]), " #Fields=2"]
+    names = {"G": " 1) Geometry, coordinate, rectangular cartesian, #Components=3",
+             "D": " 2) Dependent, field,  rectangular cartesian, #Components=4"}
+    prev = None
+    for field, label, k in comps:
+        if field != prev:
+            lines.append(names[field])
+            prev = field
+        if k is None:
+            lines.append("   %s.   %s, no modify, grid based." % (label, "*".join(["constant"] * 3)))
+            lines.append("     #xi1=0, #xi2=0, #xi3=0")
+            continue
+        lines.append("   %s.   %s, no modify, standard node based." % (label, bases[k][0]))
+        nodes = bases[k][1]
+        set_no = keys.index(k) + 1
+        first = 0 if set_no == 1 else sum(size[q] for q in keys[:set_no]) - 1
+        lines.append("     #Nodes= %d" % len(nodes))
+        for i, a in enumerate(nodes):
+            lines.append(" %5d.  #Values=1" % (a + 1))
+            lines.append("      Value indices:     1")
+            lines.append("      Scale factor indices: %4d" % (first + 1 + i))
+    p = None
+    if mesh.p_mode == 0 and x is not None:
+        p = np.asarray(x[3 * mesh.nu:], dtype=np.float64)
+    ones = {k: "  " + "   %.16E" % 1.0 * size[k] for k in keys}
     for e in range(mesh.ne):
         lines.append(" Element:            %d 0 0" % (e + 1))
-        lines.append("   Nodes:")
-        lines.append("   " + " ".join("%d" % (n + 1) for n in mesh.elem_u[e]))
-    if x is not None and mesh.p_mode == 0:
-        p = np.asarray(x[3 * mesh.nu:], dtype=np.float64)
-        lines.append(" Shape.  Dimension=3")
-        lines.append(" #Scale factor sets= 0")
-        lines.append(" #Nodes=           0")
-        lines.append(" #Fields=1")
-        lines.append(" 1) HydrostaticPressure, field, rectangular cartesian, #Components=1")
-        lines.append("   1.  l.Lagrange*l.Lagrange*l.Lagrange, no modify, grid based.")
-        lines.append("     #xi1=0, #xi2=0, #xi3=0")
-        for e in range(mesh.ne):
-            lines.append(" Element:            %d 0 0" % (e + 1))
+        if p is not None:
             lines.append("   Values:")
-            lines.append("   %.17e" % p[e])
+            lines.append("     %.16E" % p[e])
+        lines.append("   Nodes:")
+        lines.append("".join("  %10d" % (n + 1) for n in mesh.elem_u[e]))
+        lines.append("   Scale factors:")
+        lines += [ones[k] for k in keys]
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
 

@@ -1,7 +1,7 @@
-"""The reference's own exnode writer, driven the way the reference drives it
-(test infrastructure: the field-export tests compare the library's writer,
-cm_gb300/field_export.py, with this output; nothing in the library imports
-it).
+"""The reference's own exnode and exelem writers, driven the way the
+reference drives them (test infrastructure: the field-export tests compare
+the library's writer, cm_gb300/field_export.py, with this output; nothing in
+the library imports it).
 
 ``oracle/_ref/libfieldexport.so`` is the reference's src/FieldExport.c,
 compiled unchanged by ``oracle/build.py``.  This module restates, for the two
@@ -20,6 +20,24 @@ Fortran makes into it when it exports nodes:
   at the position after the node's last component);
 * FIELD_IO_NODAL_INFO_SET_SORT (:4452-4520): nodes with the same component
   set are brought together by its swap loop.
+
+For elements it restates:
+
+* FIELD_IO_EXPORT_ELEMENTS_INTO_LOCAL_FILE (field_IO_routines.f90:3533-3853):
+  group name and mesh dimensions once, then per element (in element order:
+  FIELD_IO_ELEMENTAL_INFO_SET_SORT, :3860-4061, keeps it, all elements sharing
+  their bases) the header when the element's header differs from the last,
+  the element index, the values of element-based components, the element's
+  nodes on the basis with the most nodes, and its scale factors
+  (FIELD_IO_EXPORT_ELEMENT_SCALE_FACTORS, :3418-3526: one set per distinct
+  basis, in component order; Lagrange bases have unit factors);
+* FieldIO_ExportElementalGroupHeaderFortran (:2519-3412, non-collapsed
+  branch): scale-factor sets (one per distinct basis and scaling type; the
+  default scaling, arithmetic mean), node count, field count, and per
+  component its interpolation line followed by either the grid size
+  (element-based: constant) or the node / value / scale-factor indices --
+  with the reference's first scale index of a later set,
+  SUM(set sizes up to and including that set) - 1 (:2826-2830).
 
 The fields: the geometric field (label "Geometry", rectangular cartesian
 coordinates, three components on mesh component 1) and the dependent field
@@ -129,3 +147,96 @@ def write_exnode(path, mesh, x, group="Region"):
             one[0] = mesh.X[c - 1, n] if kind == "G" else (z[c - 1, n] if c < 4 else pval[n])
             L.FieldExport_NodeValues(hd, n + 1, 1, one)
     assert L.FieldExport_CloseSession(hd) == 0
+
+
+BASIS_LAGRANGE_HERMITE_TP_TYPE = 1
+LINEAR_LAGRANGE, QUADRATIC_LAGRANGE = 1, 2
+INTERP_ELEMENT_BASED, INTERP_NODE_BASED = 2, 3
+
+
+def _components(mesh):
+    """The element components in field order: (field, component number,
+    interpolation type, basis) with basis = (name, interpolation per xi,
+    element nodes as u-node numbers per element)."""
+    nxi = mesh.nxi_u
+    u_basis = ("u", [QUADRATIC_LAGRANGE if nxi == 3 else LINEAR_LAGRANGE] * 3, mesh.elem_u)
+    comps = [("G", c, INTERP_NODE_BASED, u_basis) for c in (1, 2, 3)]
+    comps += [("D", c, INTERP_NODE_BASED, u_basis) for c in (1, 2, 3)]
+    if mesh.p_mode == 1:
+        corners = [(a * (nxi - 1)) + (b * (nxi - 1)) * nxi + (c * (nxi - 1)) * nxi * nxi
+                   for c in (0, 1) for b in (0, 1) for a in (0, 1)]
+        comps.append(("D", 4, INTERP_NODE_BASED, ("p", [LINEAR_LAGRANGE] * 3, mesh.elem_u[:, corners])))
+    else:
+        comps.append(("D", 4, INTERP_ELEMENT_BASED, u_basis))
+    return comps
+
+
+def write_exelem(path, mesh, x, group="Region"):
+    """The exelem file of the state x (element-based pressure values from x)
+    through the reference's C writer."""
+    L = lib()
+    comps = _components(mesh)
+    nu = mesh.nu
+    h = C.c_int()
+    assert L.FieldExport_OpenSession(EXPORT_TYPE_FILE, path.encode(), C.byref(h)) == 0
+    hd = h.value
+    L.FieldExport_Group(hd, group.encode())
+    L.FieldExport_MeshDimensions(hd, 3, BASIS_LAGRANGE_HERMITE_TP_TYPE)
+    # scale-factor sets: one per distinct basis (all fields use the same scaling type)
+    sets, comp_set = [], []
+    for comp in comps:
+        name = comp[3][0]
+        if name not in [b[0] for b in sets]:
+            sets.append(comp[3])
+        comp_set.append([b[0] for b in sets].index(name) + 1)
+    set_sizes = [int(np.prod([3 if t == QUADRATIC_LAGRANGE else 2 for t in b[1]])) for b in sets]
+    nmax = max(b[2].shape[1] for b in sets)
+    max_basis = next(c[3] for c in comps if c[3][2].shape[1] == nmax)
+    for e in range(mesh.ne):
+        if e == 0:  # every element has the first element's header
+            L.FieldExport_ScalingFactorCount(hd, len(sets))
+            for b, n in zip(sets, set_sizes):
+                L.FieldExport_ScaleFactors(hd, 3, (C.c_int * 3)(*b[1]), n)
+            L.FieldExport_NodeCount(hd, nmax)
+            L.FieldExport_FieldCount(hd, 2)
+            prev = None
+            for (field, cn, interp, basis), sidx in zip(comps, comp_set):
+                if field != prev:
+                    prev = field
+                    if field == "G":
+                        L.FieldExport_CoordinateVariable(hd, b"Geometry", 1, COORDINATE_RECTANGULAR_CARTESIAN_TYPE, 3)
+                    else:
+                        L.FieldExport_Variable(hd, b"Dependent", 2, FIELD_GEOMETRIC_GENERAL_TYPE, FIELD_U_VARIABLE_TYPE,
+                                               4)
+                xi = (C.c_int * 3)(*basis[1])
+                if field == "G":
+                    L.FieldExport_CoordinateComponent(hd, COORDINATE_RECTANGULAR_CARTESIAN_TYPE, cn, interp, 3, xi)
+                else:
+                    L.FieldExport_Component(hd, cn, interp, 3, xi)
+                if interp != INTERP_NODE_BASED:
+                    L.FieldExport_ElementGridSize(hd, interp, 3, xi)
+                    continue
+                first = 0 if sidx == 1 else sum(set_sizes[:sidx]) - 1
+                nn = basis[2].shape[1]
+                nodes = basis[2][e]
+                pos = [int(np.nonzero(max_basis[2][e] == n)[0][0]) + 1 for n in nodes]
+                L.FieldExport_NodeScaleIndexes(hd, nn, (C.c_int * nn)(*([1] * nn)), (C.c_int * nn)(*([1] * nn)),
+                                               (C.c_int * nn)(*pos),
+                                               (C.c_int * nn)(*range(first + 1, first + 1 + nn)))
+        L.FieldExport_ElementIndex(hd, 3, e + 1)
+        first_value = 1
+        for field, cn, interp, basis in comps:
+            if interp == INTERP_ELEMENT_BASED:
+                L.FieldExport_ElementGridValues(hd, first_value, 1, C.c_double(float(x[3 * nu + e])))
+                first_value = 0
+        nodes = max_basis[2][e] + 1
+        L.FieldExport_ElementNodeIndices(hd, len(nodes), (C.c_int * len(nodes))(*nodes.tolist()))
+        first_set, want = 1, 1
+        for (field, cn, interp, basis), sidx in zip(comps, comp_set):
+            if sidx == want:
+                want += 1
+                n = basis[2].shape[1]
+                L.FieldExport_ElementNodeScales(hd, first_set, n, (C.c_double * n)(*([1.0] * n)))
+                first_set = 0
+    assert L.FieldExport_CloseSession(hd) == 0
+

@@ -1,11 +1,11 @@
 """exnode/exelem export of a state.
 
-The exnode file is compared byte for byte with the reference's own writer,
+Both files are compared byte for byte with the reference's own writer,
 src/FieldExport.c, compiled unchanged from the reference tree
 (oracle/build.py build_ref) and driven the way the reference's
-FIELD_IO_NODES_EXPORT drives it (oracle/fieldexport_ref.py); the test is
-skipped where the reference tree is absent.  Values and element topology
-also read back exactly.
+FIELD_IO_NODES_EXPORT / FIELD_IO_ELEMENTS_EXPORT drive it
+(oracle/fieldexport_ref.py); those tests are skipped where the reference tree
+is absent.  Values and element topology also read back exactly.
 """
 import os
 
@@ -27,6 +27,21 @@ def test_exnode_matches_the_reference_writer(tmp_path, nxi, pmode):
     ours, ref = str(tmp_path / "ours.exnode"), str(tmp_path / "ref.exnode")
     F.write_exnode(ours, m, x, group="Region")
     R.write_exnode(ref, m, x, group="Region")
+    assert os.path.getsize(ref) > 0
+    assert open(ours).read() == open(ref).read()
+
+
+@pytest.mark.parametrize("nxi,pmode", [(3, "node"), (2, "element"), (2, "node"), (3, "element")])
+def test_exelem_matches_the_reference_writer(tmp_path, nxi, pmode):
+    import build as ob  # oracle/build.py
+    if ob.build_ref() is None:
+        pytest.skip("the reference tree is not on this machine")
+    import fieldexport_ref as R  # oracle/fieldexport_ref.py
+    m = M.regular_box(2, 3, 2, nxi_u=nxi, pressure=pmode, perturb=0.1, seed=4)
+    x = M.deformed_state(m, stretch=1.1, shear=0.05, noise=0.02, pressure=-1.3, seed=5)
+    ours, ref = str(tmp_path / "ours.exelem"), str(tmp_path / "ref.exelem")
+    F.write_exelem(ours, m, x, group="Region")
+    R.write_exelem(ref, m, x, group="Region")
     assert os.path.getsize(ref) > 0
     assert open(ours).read() == open(ref).read()
 
