@@ -5,7 +5,9 @@ src/FieldExport.c, compiled unchanged from the reference tree
 (oracle/build.py build_ref) and driven the way the reference's
 FIELD_IO_NODES_EXPORT / FIELD_IO_ELEMENTS_EXPORT drive it
 (oracle/fieldexport_ref.py); those tests are skipped where the reference tree
-is absent.  Values and element topology also read back exactly.
+is absent, and the files the reference writer produced for four small states,
+committed under tests/golden/field_export with the script that wrote them,
+are compared everywhere.  Values and element topology also read back exactly.
 """
 import os
 
@@ -44,6 +46,28 @@ def test_exelem_matches_the_reference_writer(tmp_path, nxi, pmode):
     R.write_exelem(ref, m, x, group="Region")
     assert os.path.getsize(ref) > 0
     assert open(ours).read() == open(ref).read()
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "field_export")
+
+
+@pytest.mark.parametrize("nxi,pmode", [(3, "node"), (2, "element"), (2, "node"), (3, "element")])
+def test_export_matches_the_golden_files(tmp_path, nxi, pmode):
+    """The committed golden files (written by the reference's own writer,
+    tests/golden/make_field_export_golden.py) against the library's writer,
+    on every machine, with or without the reference tree."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_field_export_golden", os.path.join(os.path.dirname(GOLDEN), "make_field_export_golden.py"))
+    G = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(G)
+    m, x = G.case_state(nxi, pmode)
+    base = G.case_name(nxi, pmode)
+    F.export(str(tmp_path / base), m, x, group="Region")
+    for ext in (".exnode", ".exelem"):
+        with open(os.path.join(GOLDEN, base + ext)) as f:
+            want = f.read()
+        assert open(str(tmp_path / base) + ext).read() == want, base + ext
 
 
 @pytest.mark.parametrize("nxi,pmode", [(3, "node"), (2, "element")])
