@@ -26,7 +26,6 @@
 //     computed here once.
 #include <algorithm>
 #include <array>
-#include <map>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -161,8 +160,13 @@ void sort_unique(std::vector<int32_t>& v) {
 
 template <class F>
 void parallel_for(int n, F f) {
+  // one thread per 1,024 items at most (thread start-up outweighs smaller shares)
   unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  if (n < 256) nt = 1;
+  nt = std::max(1u, std::min(nt, (unsigned)(n / 1024)));
+  if (nt == 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
   std::vector<std::thread> th;
   const int chunk = (n + (int)nt - 1) / (int)nt;
   for (unsigned t = 0; t < nt; ++t)
@@ -381,18 +385,34 @@ int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg) {
     bool isu[64];
     for (int a = 0; a < s.npe; ++a) { rn[a] = unode(e, a); isu[a] = true; }
     for (int q = 0; q < s.npp; ++q) { rn[s.npe + q] = pnode(e, q); isu[s.npe + q] = false; }
-    // ranks
+    // ranks: the column nodes of each kind in increasing order, merged with
+    // each row node's sorted neighbour list of that kind
+    int cols[2][64], ncol[2] = {0, 0};  // [u | p] local column indices, by increasing node number
+    for (int cb = 0; cb < nr; ++cb) {
+      const int k = isu[cb] ? 0 : 1;
+      int i = ncol[k]++;
+      while (i > 0 && rn[cols[k][i - 1]] > rn[cb]) {
+        cols[k][i] = cols[k][i - 1];
+        --i;
+      }
+      cols[k][i] = cb;
+    }
     for (int ra = 0; ra < nr; ++ra)
-      for (int cb = 0; cb < nr; ++cb) {
-        const std::vector<int32_t>& L = isu[ra] ? (isu[cb] ? nbu_u[rn[ra]] : nbp_u[rn[ra]])
-                                                : (isu[cb] ? nbu_p[rn[ra]] : nbp_p[rn[ra]]);
-        auto it = std::lower_bound(L.begin(), L.end(), rn[cb]);
-        if (it == L.end() || *it != rn[cb] || (it - L.begin()) > 0x7fff) { bad[e] = 1; return; }
-        T[ra * nr + cb] = (uint16_t)(it - L.begin()) | 0x8000;
+      for (int k = 0; k < 2; ++k) {
+        const std::vector<int32_t>& L = isu[ra] ? (k == 0 ? nbu_u[rn[ra]] : nbp_u[rn[ra]])
+                                                : (k == 0 ? nbu_p[rn[ra]] : nbp_p[rn[ra]]);
+        size_t j = 0;
+        for (int i = 0; i < ncol[k]; ++i) {
+          const int cb = cols[k][i];
+          while (j < L.size() && L[j] < rn[cb]) ++j;
+          if (j == L.size() || L[j] != rn[cb] || j > 0x7fff) { bad[e] = 1; return; }
+          T[ra * nr + cb] = (uint16_t)j | 0x8000;
+        }
       }
     // first-contributor bits: cleared where an element of a lower colour also
     // holds both the row node and the column node.
-    std::vector<int32_t> nbe;
+    thread_local std::vector<int32_t> nbe;  // reused: no allocation per element
+    nbe.clear();
     for (int a = 0; a < s.npe; ++a)
       for (int f : surr_u[rn[a]]) nbe.push_back(f);
     for (int q = 0; q < s.npp; ++q)
@@ -400,21 +420,15 @@ int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg) {
     sort_unique(nbe);
     for (int f : nbe) {
       if (f == e || colour[f] >= colour[e]) continue;
-      bool in[64];
+      // the row nodes of e that f also holds (f is in the sorted list of
+      // elements around each of them)
+      int shared[64], ns = 0;
       for (int r = 0; r < nr; ++r) {
-        in[r] = false;
-        if (isu[r]) {
-          for (int b = 0; b < s.npe; ++b)
-            if (unode(f, b) == rn[r]) { in[r] = true; break; }
-        } else {
-          for (int b = 0; b < s.npp; ++b)
-            if (pnode(f, b) == rn[r]) { in[r] = true; break; }
-        }
+        const std::vector<int32_t>& around = isu[r] ? surr_u[rn[r]] : surr_p[rn[r]];
+        if (std::binary_search(around.begin(), around.end(), f)) shared[ns++] = r;
       }
-      for (int ra = 0; ra < nr; ++ra)
-        if (in[ra])
-          for (int cb = 0; cb < nr; ++cb)
-            if (in[cb]) T[ra * nr + cb] &= 0x7fff;
+      for (int i = 0; i < ns; ++i)
+        for (int j = 0; j < ns; ++j) T[shared[i] * nr + shared[j]] &= 0x7fff;
     }
   });
   for (int e = 0; e < s.ne; ++e)
@@ -458,19 +472,26 @@ int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg) {
         }
       std::sort(c4.begin(), c4.end());
     };
-    std::map<std::array<int32_t, 4>, int> count;
-    std::array<int32_t, 4> c4;
-    for (int e = 0; e < s.ne; ++e)
-      for (int lf = 0; lf < 6; ++lf) {
-        corners(e, lf, c4);
-        ++count[c4];
-      }
+    // the sorted corner quadruple of every local face; a face is on the
+    // boundary when no other (element, local face) pair has the same
+    // quadruple -- every such pair holds the face's lowest corner, so only the
+    // elements around that node are compared
+    std::vector<std::array<int32_t, 4>> fc((size_t)s.ne * 6);
+    parallel_for(s.ne, [&](int e) {
+      for (int lf = 0; lf < 6; ++lf) corners(e, lf, fc[(size_t)e * 6 + lf]);
+    });
     s.bnd_mask.assign(s.ne, 0);
-    for (int e = 0; e < s.ne; ++e)
+    parallel_for(s.ne, [&](int e) {
+      uint8_t mask = 0;
       for (int lf = 0; lf < 6; ++lf) {
-        corners(e, lf, c4);
-        if (count[c4] == 1) s.bnd_mask[e] |= (uint8_t)(1u << lf);
+        const auto& c4 = fc[(size_t)e * 6 + lf];
+        int count = 0;
+        for (int f : surr_u[c4[0]])
+          for (int lg = 0; lg < 6; ++lg) count += fc[(size_t)f * 6 + lg] == c4;
+        if (count == 1) mask |= (uint8_t)(1u << lf);
       }
+      s.bnd_mask[e] = mask;
+    });
     s.bnd_ptr.assign(s.ncolours + 1, 0);
     s.bnd_elems.clear();
     for (int c = 0; c < s.ncolours; ++c) {
