@@ -276,12 +276,18 @@ int build_setup(const fe_mesh_desc* d, HostSetup& s, std::string& msg) {
   // Neighbourhoods: sorted u nodes and sorted pressure row nodes around every row node.
   std::vector<std::vector<int32_t>> nbu_u(s.nu), nbp_u(s.nu), nbu_p(s.npn), nbp_p(s.npn);
   auto fill_nb = [&](const std::vector<int32_t>& elems, std::vector<int32_t>& nu_out, std::vector<int32_t>& np_out) {
+    // gathered in per-thread scratch, stored at their final size
+    thread_local std::vector<int32_t> su, sp;
+    su.clear();
+    sp.clear();
     for (int e : elems) {
-      for (int a = 0; a < s.npe; ++a) nu_out.push_back(unode(e, a));
-      for (int q = 0; q < s.npp; ++q) np_out.push_back(pnode(e, q));
+      for (int a = 0; a < s.npe; ++a) su.push_back(unode(e, a));
+      for (int q = 0; q < s.npp; ++q) sp.push_back(pnode(e, q));
     }
-    sort_unique(nu_out);
-    sort_unique(np_out);
+    sort_unique(su);
+    sort_unique(sp);
+    nu_out.assign(su.begin(), su.end());
+    np_out.assign(sp.begin(), sp.end());
   };
   parallel_for(s.nu, [&](int n) { fill_nb(surr_u[n], nbu_u[n], nbp_u[n]); });
   parallel_for(s.npn, [&](int q) { fill_nb(surr_p[q], nbu_p[q], nbp_p[q]); });
