@@ -358,6 +358,14 @@ def _desc(m, keep):
     return d
 
 
+def _shuffled(m, seed=7):
+    """The mesh with its elements in a seeded random order."""
+    import dataclasses
+    perm = np.random.default_rng(seed).permutation(m.ne)
+    return dataclasses.replace(m, elem_u=np.ascontiguousarray(m.elem_u[perm]),
+                               elem_p=None if m.elem_p is None else np.ascontiguousarray(m.elem_p[perm]))
+
+
 def product_pattern(m, base=1):
     from cm_gb300 import _lib
     L = _lib.load()
@@ -377,6 +385,8 @@ def product_pattern(m, base=1):
     ("quad_node_3x2x4", M.regular_box(3, 2, 4, nxi_u=3, pressure="node", perturb=0.1)),
     ("lin_node", M.regular_box(3, 3, 2, nxi_u=2, pressure="node")),
     ("quad_elem", M.regular_box(2, 3, 2, nxi_u=3, pressure="element")),
+    ("cylinder", M.thick_cylinder(2, 8, 2, 0.5, 1.0, 1.0)),
+    ("quad_node_shuffled", _shuffled(M.regular_box(3, 2, 2, nxi_u=3, pressure="node", perturb=0.1))),
 ])
 def test_product_pattern_bit_exact(oracle, name, mesh):
     rp_o, col_o = oracle.Problem(mesh).pattern()
