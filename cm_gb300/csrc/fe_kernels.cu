@@ -1441,8 +1441,13 @@ int fe_jacobian_evaluate_mixed(fe_handle h, const double* x, float* values_uu, d
     if (hr && (rc = ensure((void**)&h->s_r, sizeof(double) * h->hs.ndofs))) return rc;
     if ((rc = mixed_streamed(h, dx, hu ? h->s_uu : values_uu, hc ? h->s_cp : values_coupling, hr ? h->s_r : r,
                              hu ? values_uu : nullptr, hc ? values_coupling : nullptr, hr ? r : nullptr,
-                             h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT, st)))
+                             h->high_precision == FE_HIGH_PRECISION_DOUBLE_FLOAT, st))) {
+      // launches or copies may be queued already: none may write the
+      // caller's host buffers after the call has returned
+      if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+      cudaStreamSynchronize(st);
       return rc;
+    }
     return finish_status(h, st);
   }
   if (staged && h->host_output == FE_HOST_OUTPUT_IN_PLACE) {
